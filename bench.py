@@ -1,0 +1,434 @@
+#!/usr/bin/env python3
+"""Benchmark of the fused D2Q9 step (one JSON line on rank 0).
+
+Workload (the lattice the headline metric is quoted on): D2Q9 BGK channel,
+4096 x 4096, tau = 0.56, periodic in x, half-way bounce-back walls in y, body
+force 1e-6 along x, 64 seeded circular obstacles with radius U[16, 64];
+synthetic, seeded (chemsim_gb300.workloads.channel_spec).  A "step" is one
+time step of the whole lattice; the timed region is K back-to-back steps
+(default 5000, the configuration's run length).  Inputs (1.2 GB of f32
+populations per step) are larger than L2, so no L2 flush is needed.
+
+  value   MLUPS of the f32 step, state resident in HBM, CUDA events on the
+          lattice's stream, max over ranks.
+  e2e     the same metric through the C ABI with host buffers: the initial
+          fields are uploaded from pinned host memory and, every frame of two
+          steps (the reference demo's speed_factor, src/main.rs:393), rho/u are
+          read back into pinned host memory (LBMSim::step + render,
+          src/main.rs:128-177).
+  fp16    the same lattice with half-precision deviation storage.
+  accuracy  rho/u L2 errors of the f32/f16/bf16 runs against the f64 run of
+          the same kernel after the same W + K steps.
+  roofline  algorithmic bytes (9 loads + 9 stores of 4 B + 1 B solid mask =
+          73 B per cell) / average step time against the measured HBM copy
+          bandwidth.
+
+--impl reference times the CPU implementation of the same step, restated op
+by op the way lbm.rs drives ArrayFire (oracle/, the reference cannot be built
+on this machine), on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+BYTES_F32 = 72          # 9 loads + 9 stores x 4 B
+BYTES_F16 = 36
+BYTES_MASK = 1          # u8 solid mask read once per cell
+WORKLOAD = "channel_4096x4096_tau0.56_walls_y_periodic_x_force1e-6_64obstacles_r16-64"
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5000)
+    p.add_argument("--warmup", type=int, default=20)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--size", type=int, default=4096)
+    p.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
+    p.add_argument("--no-accuracy", action="store_true")
+    p.add_argument("--strict", action="store_true",
+                   help="time the reference operation order instead of LBM_FAST")
+    return p.parse_args()
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0")),
+            int(os.environ.get("WORLD_SIZE", "1")))
+
+
+# ---------------------------------------------------------------------------
+# clocks
+# ---------------------------------------------------------------------------
+
+class ClockSampler:
+    """nvidia-smi sampled every 200 ms while the timed region runs."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.tmp = None
+
+    def start(self):
+        try:
+            self.tmp = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.tmp, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.tmp.flush()
+        self.tmp.seek(0)
+        rows = [r.split(",") for r in self.tmp.read().splitlines() if r.strip()]
+        os.unlink(self.tmp.name)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [x.strip() for x in r]
+            try:
+                sm.append(float(r[0]))
+                mx.append(float(r[1]))
+            except (ValueError, IndexError):
+                continue
+            for name, val in zip(names, r[4:8]):
+                if val.lower() in ("active", "1"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# helpers
+# ---------------------------------------------------------------------------
+
+def measured_peak_gbs():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profiled_traffic(kernel_tag: str):
+    """DRAM bytes per cell of the step kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", f"{kernel_tag}.txt")
+    try:
+        with open(path) as fh:
+            m = re.search(r"dram_bytes_per_cell:\s*([0-9.]+)", fh.read())
+        return float(m.group(1)) if m else None
+    except OSError:
+        return None
+
+
+def l2_rel(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def make_lattice(spec, precision, flags):
+    from chemsim_gb300 import lbm
+    lat = lbm.Lattice(spec.w, spec.h, spec.tau, precision, flags)
+    lat.set_force(*spec.force)
+    lat.set_geometry(spec.solid)
+    lat.init_equilibrium(spec.rho, spec.ux, spec.uy)
+    return lat
+
+
+def timed_steps(lat, steps, warmup, torch, stream, dist=None):
+    """W untimed steps, then exactly K steps between CUDA events on the
+    lattice's stream; returns elapsed seconds (max over ranks)."""
+    lat.set_stream(stream.cuda_stream)
+    lat.step(warmup)
+    lat.synchronize()
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    start = torch.cuda.Event(enable_timing=True)
+    end = torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    lat.step(steps)
+    end.record(stream)
+    end.synchronize()
+    torch.cuda.synchronize()
+    secs = start.elapsed_time(end) / 1e3
+    if dist is not None:
+        t = torch.tensor([secs], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        secs = float(t.item())
+    return secs
+
+
+def cpu_sample(spec, steps, threads, structured=True):
+    """The oracle's CPU step on the full lattice, `steps` steps; MLUPS."""
+    import oracle
+    f0 = oracle.equilibrium(spec.rho, spec.ux, spec.uy)
+    oracle.step(f0[:, :64], 1, tau=spec.tau, flags=spec.flags, solid=spec.solid[:64],
+                force=spec.force, structured=structured, threads=threads)
+    t0 = time.perf_counter()
+    oracle.step(f0, steps, tau=spec.tau, flags=spec.flags, solid=spec.solid,
+                force=spec.force, structured=structured, threads=threads)
+    secs = time.perf_counter() - t0
+    return spec.w * spec.h * steps / secs / 1e6, secs
+
+
+# ---------------------------------------------------------------------------
+# reference arm
+# ---------------------------------------------------------------------------
+
+def run_reference(args):
+    rank, _, world = dist_env()
+    if rank != 0:
+        return 0
+    import oracle
+    from chemsim_gb300.workloads import channel_spec
+    oracle.build()
+    threads = os.cpu_count() or 1
+    full = channel_spec(args.size)
+    # Calibrate on a 512-row band, then size the band so W + K steps take
+    # about 90 s of host time.
+    band = 512
+    spec = crop(full, band)
+    f = oracle.equilibrium(spec.rho, spec.ux, spec.uy)
+    t0 = time.perf_counter()
+    f = oracle.step(f, 2, tau=spec.tau, flags=spec.flags, solid=spec.solid, force=spec.force,
+                    structured=True, threads=threads)
+    per_cell = (time.perf_counter() - t0) / (2 * spec.w * spec.h)
+    budget = 90.0
+    rows = int(budget / max(per_cell * spec.w * (args.steps + args.warmup), 1e-12))
+    rows = max(16, min(full.h, rows))
+    spec = crop(full, rows)
+    f = oracle.equilibrium(spec.rho, spec.ux, spec.uy)
+    f = oracle.step(f, args.warmup, tau=spec.tau, flags=spec.flags, solid=spec.solid,
+                    force=spec.force, structured=True, threads=threads)
+    t0 = time.perf_counter()
+    oracle.step(f, args.steps, tau=spec.tau, flags=spec.flags, solid=spec.solid,
+                force=spec.force, structured=True, threads=threads)
+    secs = time.perf_counter() - t0
+    mlups = spec.w * spec.h * args.steps / secs / 1e6
+    sample = (f"{args.steps} time steps of a {spec.w}x{spec.h} band (rows 0..{spec.h - 1}) of "
+              f"the {full.w}x{full.h} channel lattice, same tau/force/walls/obstacles; f32, "
+              "op-by-op full-plane passes as lbm.rs drives ArrayFire (oracle/lbm_oracle.cpp "
+              "step_structured), OpenMP")
+    line = {
+        "metric": "D2Q9 MLUPS", "value": round(mlups, 3), "unit": "MLUPS", "impl": "reference",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": secs / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "sample_rows": spec.h, "parallelism": "cpu"},
+        "cpu_baseline": {"value": round(mlups, 3), "unit": "MLUPS", "cores": threads,
+                         "kind": "port", "sample": sample},
+        "e2e": {"value": round(mlups, 3), "unit": "MLUPS", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "note": "taktoa/chemsim (Rust over ArrayFire 3.6) cannot be built here: no Rust "
+                "toolchain and no ArrayFire; timed is the oracle's restatement of its step",
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def crop(spec, rows):
+    from chemsim_gb300.workloads import LatticeSpec
+    r = min(rows, spec.h)
+    return LatticeSpec(spec.w, r, spec.tau, spec.flags, force=spec.force,
+                       solid=np.ascontiguousarray(spec.solid[:r]),
+                       rho=np.ascontiguousarray(spec.rho[:r]),
+                       ux=np.ascontiguousarray(spec.ux[:r]),
+                       uy=np.ascontiguousarray(spec.uy[:r]), name=spec.name + f"_band{r}")
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
+
+def run_ours(args):
+    import torch
+    rank, local_rank, world = dist_env()
+    dist = None
+    if world > 1:
+        import torch.distributed as tdist
+        torch.cuda.set_device(local_rank)
+        tdist.init_process_group("nccl")
+        dist = tdist
+    else:
+        torch.cuda.set_device(0)
+    from chemsim_gb300 import build, lbm
+    from chemsim_gb300.workloads import channel_spec
+    build()
+
+    spec = channel_spec(args.size)
+    cells = spec.w * spec.h
+    base_flags = spec.flags | (0 if args.strict else lbm.FAST)
+    stream = torch.cuda.Stream()
+    clocks = ClockSampler(torch.cuda.current_device())
+
+    # f32: the headline
+    lat32 = make_lattice(spec, lbm.F32, base_flags)
+    clocks.start()
+    t32 = timed_steps(lat32, args.steps, args.warmup, torch, stream, dist)
+    # f16 deviation storage
+    lat16 = make_lattice(spec, lbm.F16DEV, base_flags)
+    t16 = timed_steps(lat16, args.steps, args.warmup, torch, stream, dist)
+    clk = clocks.stop()
+    mlups32 = cells * args.steps / t32 / 1e6 * world
+    mlups16 = cells * args.steps / t16 / 1e6 * world
+
+    accuracy = None
+    if not args.no_accuracy:
+        m32 = lat32.moments()
+        m16 = lat16.moments()
+        latb = make_lattice(spec, lbm.BF16DEV, base_flags)
+        latb.step(args.warmup + args.steps)
+        mb = latb.moments()
+        latb.close()
+        lat64 = make_lattice(spec, lbm.F64, base_flags)
+        lat64.step(args.warmup + args.steps)
+        m64 = lat64.moments()
+        lat64.close()
+        fluid = spec.solid == 0
+
+        def errs(m):
+            return {"rho_dev_l2": l2_rel(m[0][fluid] - 1.0, m64[0][fluid] - 1.0),
+                    "rho_l2": l2_rel(m[0][fluid], m64[0][fluid]),
+                    "u_l2": l2_rel(np.stack([m[1][fluid], m[2][fluid]]),
+                                   np.stack([m64[1][fluid], m64[2][fluid]]))}
+        accuracy = {"steps": args.warmup + args.steps, "against": "f64 run of the same kernel",
+                    "f32": errs(m32), "f16dev": errs(m16), "bf16dev": errs(mb),
+                    "u_rms_f64": float(np.sqrt(np.mean(m64[1][fluid] ** 2 + m64[2][fluid] ** 2)))}
+    lat32.close()
+    lat16.close()
+
+    # e2e through the C ABI with pinned host buffers
+    e2e = run_e2e(spec, args, torch, dist)
+
+    peak, peak_kind = measured_peak_gbs()
+    bpc = BYTES_F32 + BYTES_MASK
+    step_s = t32 / args.steps
+    achieved = bpc * cells / step_s / 1e9
+    traffic_pc = profiled_traffic("lbm_step_f32_channel")
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4),
+                "traffic": None if traffic_pc is None else round(traffic_pc * cells / 1e9, 4),
+                "algorithmic_bytes_per_cell": bpc, "peak_source": peak_kind,
+                "traffic_unit": "GB per launch"}
+    fp16 = {"mlups": round(mlups16, 1), "speedup_vs_f32": round(mlups16 / mlups32, 3),
+            "achieved_gbs": round((BYTES_F16 + BYTES_MASK) * cells / (t16 / args.steps) / 1e9, 1)}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        import oracle
+        oracle.build()
+        v, secs = cpu_sample(spec, 3, threads, structured=True)
+        vf, _ = cpu_sample(spec, 3, threads, structured=False)
+        cpu = {"value": round(v, 3), "unit": "MLUPS", "cores": threads, "kind": "port",
+               "sample": f"3 full {spec.w}x{spec.h} time steps ({secs:.1f} s), f32, the oracle's "
+                         "op-by-op restatement of lbm.rs's ArrayFire passes, OpenMP",
+               "fused_cpu_mlups": round(vf, 3)}
+
+    if rank == 0:
+        line = {
+            "metric": "D2Q9 MLUPS", "value": round(mlups32, 1), "unit": "MLUPS",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(step_s * 1e3, 5), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "cells": cells,
+                       "arithmetic": "reference order" if args.strict else "LBM_FAST (FMA)",
+                       "l2": "inputs larger than L2 (1.2 GB of populations per step); no flush",
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "hbm_gbs": round(achieved, 1),
+            "roofline": roofline,
+            "fp16": fp16,
+            "accuracy": accuracy,
+            "e2e": e2e,
+            "gpu_launches": args.steps,
+            "clocks": clk,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def run_e2e(spec, args, torch, dist):
+    """K steps through the C ABI: upload fields from pinned host memory, then
+    frames of 2 steps each followed by a rho/u readback to pinned memory."""
+    from chemsim_gb300 import lbm
+    flags = spec.flags | (0 if args.strict else lbm.FAST)
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()  # noqa: E731
+    rho, ux, uy = pin(spec.rho), pin(spec.ux), pin(spec.uy)
+    out = [torch.empty((spec.h, spec.w), dtype=torch.float32).pin_memory().numpy() for _ in range(3)]
+    lat = lbm.Lattice(spec.w, spec.h, spec.tau, lbm.F32, flags)
+    lat.set_force(*spec.force)
+    lat.set_geometry(spec.solid)
+    lat.init_equilibrium(rho, ux, uy)
+    lat.step(args.warmup)
+    lat.synchronize()
+    frames = max(1, args.steps // 2)
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    lat.init_equilibrium(rho, ux, uy)
+    for _ in range(frames):
+        lat.step_moments(2)
+        lib = lat._lib
+        from chemsim_gb300._lib import check
+        check(lib.lbm_read_moments(lat.handle, out[0].ctypes.data, out[1].ctypes.data,
+                                   out[2].ctypes.data, 0))
+    lat.synchronize()
+    secs = time.perf_counter() - t0
+    if dist is not None:
+        t = torch.tensor([secs], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        secs = float(t.item())
+    lat.close()
+    world = dist.get_world_size() if dist is not None else 1
+    cells = spec.w * spec.h
+    steps = 2 * frames
+    return {"value": round(cells * steps / secs / 1e6 * world, 1), "unit": "MLUPS",
+            "h2d_bytes_per_step": int(3 * 4 * cells / steps),
+            "d2h_bytes_per_step": int(3 * 4 * cells / 2),
+            "frames": frames, "steps_per_frame": 2,
+            "note": "h2d: rho/ux/uy fields once per run, amortised; d2h: rho/ux/uy every frame"}
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

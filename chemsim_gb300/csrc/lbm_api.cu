@@ -1,0 +1,637 @@
+// lbm_api.cu — the C ABI of include/lbm_cuda.h for single lattices.
+//
+// A handle replaces the reference's State<D2Q9> (taktoa/chemsim
+// src/lbm.rs:670-819): it owns two device population buffers (A/B
+// ping-pong), the solid mask, the moment buffers and one CUDA stream.
+// State::step's three phases (:694-714) are one fused kernel launch per step;
+// runs of steps replay a captured CUDA graph.
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <type_traits>
+
+#include "lbm_aux.cuh"
+
+using namespace lbmk;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+    return fail(e == cudaErrorMemoryAllocation ? LBM_ERR_OUT_OF_MEMORY : LBM_ERR_CUDA,
+                std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define LBM_CUDA(expr)                                   \
+    do {                                                 \
+        cudaError_t e__ = (expr);                        \
+        if (e__ != cudaSuccess) return cuda_fail(e__, #expr); \
+    } while (0)
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev) {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceGuard() {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
+
+constexpr int kGraphSteps = 64;       // steps per captured graph (even)
+constexpr int kHealthBlocks = 1024;
+constexpr int kMaxSide = 65535 * 4;    // grid.y limit x 4 rows per block
+
+size_t elem_size(int precision) {
+    switch (precision) {
+        case LBM_F32: return 4;
+        case LBM_F64: return 8;
+        case LBM_F16DEV:
+        case LBM_BF16DEV: return 2;
+        default: return 0;
+    }
+}
+
+int default_cells(int precision) {
+    switch (precision) {
+        case LBM_F32: return 4;
+        case LBM_F64: return 2;
+        default: return 8;
+    }
+}
+
+bool valid_cells(int precision, int v) {
+    switch (precision) {
+        case LBM_F32: return v == 4 || v == 8;
+        case LBM_F64: return v == 2;
+        default: return v == 8;
+    }
+}
+
+int grid_for(int64_t n, int block) {
+    int64_t g = (n + block - 1) / block;
+    if (g > 65535 * 8) g = 65535 * 8;
+    return int(g < 1 ? 1 : g);
+}
+
+}  // namespace
+
+struct lbm_lattice {
+    int w = 0, h = 0, precision = 0, flags = 0;
+    int pitch = 0, mpitch = 0;
+    int64_t plane = 0;
+    size_t esize = 0;
+    void* buf[2] = {nullptr, nullptr};
+    int cur = 0;
+    uint8_t* solid = nullptr;
+    bool has_solid = false;
+    float* mom[3] = {nullptr, nullptr, nullptr};
+    bool mom_valid = false;
+    void* staging = nullptr;
+    size_t staging_bytes = 0;
+    HealthPartial* health = nullptr;      // kHealthBlocks partials + 1 result
+    int collision = LBM_COLLISION_BGK;
+    float tau = 1.f, tau_minus = 1.f, dx = 1.f, dt = 1.f, fx = 0.f, fy = 0.f;
+    float time = 0.f;
+    int64_t steps = 0;
+    cudaStream_t own = nullptr, stream = nullptr;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    bool dirty = true;
+    int vcells = 0, rows = 4;
+    int dev = 0;
+};
+
+namespace {
+
+// Collision constants exactly as src/lbm.rs computes them in its Scalar type
+// (weights :205-215, cs :83-85, equilibrium factors :54-66, BGK :357, TRT
+// :430-441).  Host code is built with -ffp-contract=off.
+template <class CT>
+Consts<CT> make_consts(const lbm_lattice* L) {
+    Consts<CT> c{};
+    const CT n[9] = {CT(16), CT(4), CT(4), CT(4), CT(4), CT(1), CT(1), CT(1), CT(1)};
+    for (int i = 0; i < 9; ++i) c.wt[i] = n[i] / CT(36);
+    const CT dx = CT(L->dx), dt = CT(L->dt);
+    const CT cs = dx / (CT(std::sqrt(CT(3))) * dt);
+    const CT cs2 = cs * cs;
+    const CT cs4 = cs2 * cs2;
+    c.k1 = CT(1) / cs2;
+    c.k2 = CT(1) / (CT(2) * cs4);
+    c.k3 = CT(-1) / (CT(2) * cs2);
+    const CT tau = CT(L->tau);
+    c.bgk_factor = -dt / tau;
+    c.omega_p = CT(1) / tau;
+    c.omega_m = CT(1) / CT(L->tau_minus);
+    c.trt_scale = -dt * CT(0.5);
+    c.fx = CT(L->fx);
+    c.fy = CT(L->fy);
+    c.hfx = c.fx * CT(0.5);
+    c.hfy = c.fy * CT(0.5);
+    c.guo = CT(1) - CT(1) / (CT(2) * tau);
+    c.inv_cs4 = CT(1) / cs4;
+    c.force = (L->fx != 0.f || L->fy != 0.f) ? 1 : 0;
+    c.collision = L->collision;
+    if (L->precision == LBM_F16DEV) { c.dscale = CT(kHalfDevScale); c.dinv = CT(1) / CT(kHalfDevScale); }
+    else if (L->precision == LBM_BF16DEV) { c.dscale = CT(kBf16DevScale); c.dinv = CT(1) / CT(kBf16DevScale); }
+    else { c.dscale = CT(1); c.dinv = CT(1); }
+    return c;
+}
+
+template <class S>
+cudaError_t launch_one_t(lbm_lattice* L, int from, bool moments) {
+    using CT = typename Store<S>::CT;
+    StepArgs<CT> a{};
+    a.src = L->buf[from];
+    a.dst = L->buf[from ^ 1];
+    a.solid = L->has_solid ? L->solid : nullptr;
+    if (moments) { a.mom_rho = L->mom[0]; a.mom_ux = L->mom[1]; a.mom_uy = L->mom[2]; }
+    a.w = L->w; a.h = L->h; a.pitch = L->pitch; a.mpitch = L->mpitch; a.plane = L->plane;
+    a.flags = L->flags;
+    a.c = make_consts<CT>(L);
+    return launch_step<S>(a, (L->flags & LBM_FRAME_XY) ? 1 : 0, (L->flags & LBM_FAST) != 0,
+                          L->vcells, L->rows, L->stream);
+}
+
+cudaError_t launch_one(lbm_lattice* L, int from, bool moments) {
+    switch (L->precision) {
+        case LBM_F32: return launch_one_t<float>(L, from, moments);
+        case LBM_F64: return launch_one_t<double>(L, from, moments);
+        case LBM_F16DEV: return launch_one_t<__half>(L, from, moments);
+        default: return launch_one_t<__nv_bfloat16>(L, from, moments);
+    }
+}
+
+void drop_graphs(lbm_lattice* L) {
+    for (auto& g : L->graph) {
+        if (g) cudaGraphExecDestroy(g);
+        g = nullptr;
+    }
+}
+
+int ensure_graph(lbm_lattice* L) {
+    if (L->dirty) { drop_graphs(L); L->dirty = false; }
+    if (L->graph[L->cur]) return LBM_OK;
+    LBM_CUDA(cudaStreamBeginCapture(L->stream, cudaStreamCaptureModeThreadLocal));
+    int from = L->cur;
+    cudaError_t err = cudaSuccess;
+    for (int s = 0; s < kGraphSteps && err == cudaSuccess; ++s) {
+        err = launch_one(L, from, false);
+        from ^= 1;
+    }
+    cudaGraph_t g = nullptr;
+    cudaError_t e2 = cudaStreamEndCapture(L->stream, &g);
+    if (err != cudaSuccess) { if (g) cudaGraphDestroy(g); return cuda_fail(err, "step capture"); }
+    if (e2 != cudaSuccess) return cuda_fail(e2, "cudaStreamEndCapture");
+    cudaError_t e3 = cudaGraphInstantiate(&L->graph[L->cur], g, 0);
+    cudaGraphDestroy(g);
+    if (e3 != cudaSuccess) { L->graph[L->cur] = nullptr; return cuda_fail(e3, "cudaGraphInstantiate"); }
+    return LBM_OK;
+}
+
+int ensure_staging(lbm_lattice* L, size_t bytes) {
+    if (L->staging_bytes >= bytes) return LBM_OK;
+    if (L->staging) cudaFree(L->staging);
+    L->staging = nullptr;
+    L->staging_bytes = 0;
+    LBM_CUDA(cudaMalloc(&L->staging, bytes));
+    L->staging_bytes = bytes;
+    return LBM_OK;
+}
+
+template <class S, class IN>
+int set_pops_t(lbm_lattice* L, const IN* f) {
+    using CT = typename Store<S>::CT;
+    const Consts<CT> c = make_consts<CT>(L);
+    const int64_t n = int64_t(L->w) * L->h;
+    S* dst = static_cast<S*>(L->buf[L->cur]);
+    if constexpr (std::is_same<S, IN>::value) {
+        for (int i = 0; i < 9; ++i)
+            LBM_CUDA(cudaMemcpy2DAsync(dst + i * L->plane, size_t(L->pitch) * sizeof(S), f + i * n,
+                                       size_t(L->w) * sizeof(IN), size_t(L->w) * sizeof(IN), L->h,
+                                       cudaMemcpyHostToDevice, L->stream));
+    } else {
+        int rc = ensure_staging(L, size_t(n) * sizeof(IN));
+        if (rc) return rc;
+        IN* st = static_cast<IN*>(L->staging);
+        for (int i = 0; i < 9; ++i) {
+            LBM_CUDA(cudaMemcpyAsync(st, f + i * n, size_t(n) * sizeof(IN), cudaMemcpyHostToDevice,
+                                     L->stream));
+            pack_kernel<S, IN><<<grid_for(n, 256), 256, 0, L->stream>>>(
+                dst + i * L->plane, st, L->w, L->h, L->pitch, c.wt[i], c.dscale);
+            LBM_CUDA(cudaGetLastError());
+        }
+    }
+    LBM_CUDA(cudaStreamSynchronize(L->stream));
+    return LBM_OK;
+}
+
+template <class S, class OUT>
+int get_pops_t(lbm_lattice* L, OUT* f) {
+    using CT = typename Store<S>::CT;
+    const Consts<CT> c = make_consts<CT>(L);
+    const int64_t n = int64_t(L->w) * L->h;
+    const S* src = static_cast<const S*>(L->buf[L->cur]);
+    if constexpr (std::is_same<S, OUT>::value) {
+        for (int i = 0; i < 9; ++i)
+            LBM_CUDA(cudaMemcpy2DAsync(f + i * n, size_t(L->w) * sizeof(OUT), src + i * L->plane,
+                                       size_t(L->pitch) * sizeof(S), size_t(L->w) * sizeof(OUT),
+                                       L->h, cudaMemcpyDeviceToHost, L->stream));
+    } else {
+        int rc = ensure_staging(L, size_t(n) * sizeof(OUT));
+        if (rc) return rc;
+        OUT* st = static_cast<OUT*>(L->staging);
+        for (int i = 0; i < 9; ++i) {
+            unpack_kernel<S, OUT><<<grid_for(n, 256), 256, 0, L->stream>>>(
+                st, src + i * L->plane, L->w, L->h, L->pitch, c.wt[i], c.dinv);
+            LBM_CUDA(cudaGetLastError());
+            LBM_CUDA(cudaMemcpyAsync(f + i * n, st, size_t(n) * sizeof(OUT), cudaMemcpyDeviceToHost,
+                                     L->stream));
+        }
+    }
+    LBM_CUDA(cudaStreamSynchronize(L->stream));
+    return LBM_OK;
+}
+
+template <class S>
+int eq_init_t(lbm_lattice* L) {
+    using CT = typename Store<S>::CT;
+    const int64_t n = int64_t(L->w) * L->h;
+    eq_init_kernel<S><<<grid_for(n, 256), 256, 0, L->stream>>>(
+        static_cast<S*>(L->buf[L->cur]), L->mom[0], L->mom[1], L->mom[2], L->w, L->h, L->pitch,
+        L->plane, make_consts<CT>(L));
+    LBM_CUDA(cudaGetLastError());
+    return LBM_OK;
+}
+
+template <class S>
+int fill_rest_t(lbm_lattice* L, int which) {
+    using CT = typename Store<S>::CT;
+    fill_rest_kernel<S><<<grid_for(L->plane, 256), 256, 0, L->stream>>>(
+        static_cast<S*>(L->buf[which]), L->plane, make_consts<CT>(L));
+    LBM_CUDA(cudaGetLastError());
+    return LBM_OK;
+}
+
+template <class S>
+int moments_t(lbm_lattice* L) {
+    using CT = typename Store<S>::CT;
+    const int64_t n = int64_t(L->w) * L->h;
+    moments_kernel<S><<<grid_for(n, 256), 256, 0, L->stream>>>(
+        static_cast<const S*>(L->buf[L->cur]), L->mom[0], L->mom[1], L->mom[2], L->w, L->h,
+        L->pitch, L->plane, L->pitch, make_consts<CT>(L));
+    LBM_CUDA(cudaGetLastError());
+    return LBM_OK;
+}
+
+template <class S>
+int health_t(lbm_lattice* L) {
+    using CT = typename Store<S>::CT;
+    health_kernel<S><<<kHealthBlocks, 256, 0, L->stream>>>(
+        static_cast<const S*>(L->buf[L->cur]), L->w, L->h, L->pitch, L->plane,
+        make_consts<CT>(L), L->health);
+    LBM_CUDA(cudaGetLastError());
+    health_final_kernel<<<1, 32, 0, L->stream>>>(L->health, kHealthBlocks, L->health + kHealthBlocks);
+    LBM_CUDA(cudaGetLastError());
+    return LBM_OK;
+}
+
+#define LBM_DISPATCH(L, fn, ...)                                        \
+    ((L)->precision == LBM_F32    ? fn<float>(__VA_ARGS__)              \
+     : (L)->precision == LBM_F64  ? fn<double>(__VA_ARGS__)             \
+     : (L)->precision == LBM_F16DEV ? fn<__half>(__VA_ARGS__)           \
+                                    : fn<__nv_bfloat16>(__VA_ARGS__))
+
+int check_handle(const lbm_lattice* L) {
+    if (!L) return fail(LBM_ERR_INVALID_ARGUMENT, "null lattice handle");
+    return LBM_OK;
+}
+
+int steps_impl(lbm_lattice* L, int nsteps, bool moments) {
+    if (nsteps < 0) return fail(LBM_ERR_INVALID_ARGUMENT, "nsteps must be >= 0");
+    if (nsteps == 0) return LBM_OK;
+    const int plain = moments ? nsteps - 1 : nsteps;
+    const int full = plain / kGraphSteps;
+    const int rem = plain % kGraphSteps;
+    if (full > 0) {
+        int rc = ensure_graph(L);
+        if (rc) return rc;
+        for (int k = 0; k < full; ++k) LBM_CUDA(cudaGraphLaunch(L->graph[L->cur], L->stream));
+    }
+    for (int k = 0; k < rem; ++k) {
+        LBM_CUDA(launch_one(L, L->cur, false));
+        L->cur ^= 1;
+    }
+    if (moments) {
+        LBM_CUDA(launch_one(L, L->cur, true));
+        L->cur ^= 1;
+    }
+    // State::step: time += delta_t once per step, in f32 (src/lbm.rs:713).
+    for (int k = 0; k < nsteps; ++k) L->time += L->dt;
+    L->steps += nsteps;
+    L->mom_valid = moments;
+    return LBM_OK;
+}
+
+}  // namespace
+
+namespace lbmk {
+__global__ void health_final_kernel(const HealthPartial* __restrict__ partial, int nblocks,
+                                    HealthPartial* __restrict__ out) {
+    if (threadIdx.x != 0) return;
+    HealthPartial p{0.0, 0.0, 0.0, INFINITY, INFINITY, 0};
+    for (int k = 0; k < nblocks; ++k) {
+        p.mass += partial[k].mass;
+        p.mx += partial[k].mx;
+        p.my += partial[k].my;
+        p.minf = fmin(p.minf, partial[k].minf);
+        p.mineq0 = fmin(p.mineq0, partial[k].mineq0);
+        p.nonfinite += partial[k].nonfinite;
+    }
+    *out = p;
+}
+}  // namespace lbmk
+
+extern "C" {
+
+const char* lbm_last_error_string(void) { return g_err.c_str(); }
+
+int lbm_version(void) { return 100; }
+
+int lbm_create(int w, int h, float tau, int precision, int flags, lbm_lattice** out) {
+    if (!out) return fail(LBM_ERR_INVALID_ARGUMENT, "out must not be null");
+    *out = nullptr;
+    if (w < 1 || h < 1 || w > kMaxSide || h > kMaxSide)
+        return fail(LBM_ERR_INVALID_ARGUMENT, "lattice sides must be in [1, 262140]");
+    if (!(tau > 0.f) || !std::isfinite(tau))
+        return fail(LBM_ERR_INVALID_ARGUMENT, "tau must be finite and > 0");
+    const size_t es = elem_size(precision);
+    if (!es) return fail(LBM_ERR_INVALID_ARGUMENT, "unknown precision");
+    if ((flags & 3) == 3 || ((flags >> 2) & 3) == 3 || (flags & ~0x7f))
+        return fail(LBM_ERR_INVALID_ARGUMENT, "invalid boundary flags");
+    int dev = 0;
+    LBM_CUDA(cudaGetDevice(&dev));
+    lbm_lattice* L = new lbm_lattice();
+    L->w = w; L->h = h; L->precision = precision; L->flags = flags; L->tau = tau;
+    L->esize = es;
+    L->dev = dev;
+    const int per128 = int(128 / es);
+    L->pitch = (w + per128 - 1) / per128 * per128;
+    L->mpitch = (w + 127) / 128 * 128;
+    L->plane = int64_t(L->pitch) * h;
+    L->vcells = default_cells(precision);
+    L->rows = 4;
+    auto cleanup = [&](int rc) { lbm_destroy(L); return rc; };
+    cudaError_t e;
+    for (int b = 0; b < 2; ++b) {
+        e = cudaMalloc(&L->buf[b], size_t(9) * L->plane * es);
+        if (e != cudaSuccess) return cleanup(cuda_fail(e, "population buffer"));
+    }
+    for (int m = 0; m < 3; ++m) {
+        e = cudaMalloc(reinterpret_cast<void**>(&L->mom[m]), size_t(L->plane) * sizeof(float));
+        if (e != cudaSuccess) return cleanup(cuda_fail(e, "moment buffer"));
+    }
+    e = cudaMalloc(reinterpret_cast<void**>(&L->health), sizeof(HealthPartial) * (kHealthBlocks + 1));
+    if (e != cudaSuccess) return cleanup(cuda_fail(e, "health scratch"));
+    e = cudaStreamCreateWithFlags(&L->own, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return cleanup(cuda_fail(e, "stream"));
+    L->stream = L->own;
+    for (int b = 0; b < 2; ++b) {
+        int rc = LBM_DISPATCH(L, fill_rest_t, L, b);
+        if (rc) return cleanup(rc);
+    }
+    e = cudaStreamSynchronize(L->stream);
+    if (e != cudaSuccess) return cleanup(cuda_fail(e, "create"));
+    *out = L;
+    return LBM_OK;
+}
+
+int lbm_destroy(lbm_lattice* L) {
+    if (!L) return LBM_OK;
+    {
+        DeviceGuard g(L->dev);
+        if (L->stream) cudaStreamSynchronize(L->stream);
+        drop_graphs(L);
+        for (auto& b : L->buf) if (b) cudaFree(b);
+        for (auto& m : L->mom) if (m) cudaFree(m);
+        if (L->solid) cudaFree(L->solid);
+        if (L->staging) cudaFree(L->staging);
+        if (L->health) cudaFree(L->health);
+        if (L->own) cudaStreamDestroy(L->own);
+    }
+    delete L;
+    return LBM_OK;
+}
+
+int lbm_set_discretization(lbm_lattice* L, float dx, float dt) {
+    if (int rc = check_handle(L)) return rc;
+    if (!(dx > 0.f) || !(dt > 0.f) || !std::isfinite(dx) || !std::isfinite(dt))
+        return fail(LBM_ERR_INVALID_ARGUMENT, "delta_x and delta_t must be finite and > 0");
+    L->dx = dx; L->dt = dt; L->dirty = true; L->mom_valid = false;
+    return LBM_OK;
+}
+
+int lbm_set_collision(lbm_lattice* L, int kind, float tau, float tau_minus) {
+    if (int rc = check_handle(L)) return rc;
+    if (kind != LBM_COLLISION_BGK && kind != LBM_COLLISION_TRT)
+        return fail(LBM_ERR_INVALID_ARGUMENT, "unknown collision operator");
+    if (!(tau > 0.f) || !std::isfinite(tau))
+        return fail(LBM_ERR_INVALID_ARGUMENT, "tau must be finite and > 0");
+    if (kind == LBM_COLLISION_TRT && (!(tau_minus > 0.f) || !std::isfinite(tau_minus)))
+        return fail(LBM_ERR_INVALID_ARGUMENT, "tau_minus must be finite and > 0");
+    L->collision = kind; L->tau = tau;
+    L->tau_minus = kind == LBM_COLLISION_TRT ? tau_minus : 1.f;
+    L->dirty = true;
+    return LBM_OK;
+}
+
+int lbm_init_equilibrium(lbm_lattice* L, const float* rho, const float* ux, const float* uy) {
+    if (int rc = check_handle(L)) return rc;
+    if (!rho || !ux || !uy) return fail(LBM_ERR_INVALID_ARGUMENT, "null field pointer");
+    DeviceGuard g(L->dev);
+    const float* src[3] = {rho, ux, uy};
+    for (int m = 0; m < 3; ++m)
+        LBM_CUDA(cudaMemcpy2DAsync(L->mom[m], size_t(L->pitch) * 4, src[m], size_t(L->w) * 4,
+                                   size_t(L->w) * 4, L->h, cudaMemcpyHostToDevice, L->stream));
+    if (int rc = LBM_DISPATCH(L, eq_init_t, L)) return rc;
+    LBM_CUDA(cudaStreamSynchronize(L->stream));
+    L->mom_valid = false;
+    return LBM_OK;
+}
+
+int lbm_set_populations(lbm_lattice* L, const float* f) {
+    if (int rc = check_handle(L)) return rc;
+    if (!f) return fail(LBM_ERR_INVALID_ARGUMENT, "null population pointer");
+    DeviceGuard g(L->dev);
+    L->mom_valid = false;
+    switch (L->precision) {
+        case LBM_F32: return set_pops_t<float, float>(L, f);
+        case LBM_F64: return set_pops_t<double, float>(L, f);
+        case LBM_F16DEV: return set_pops_t<__half, float>(L, f);
+        default: return set_pops_t<__nv_bfloat16, float>(L, f);
+    }
+}
+
+int lbm_get_populations(lbm_lattice* L, float* f) {
+    if (int rc = check_handle(L)) return rc;
+    if (!f) return fail(LBM_ERR_INVALID_ARGUMENT, "null population pointer");
+    DeviceGuard g(L->dev);
+    switch (L->precision) {
+        case LBM_F32: return get_pops_t<float, float>(L, f);
+        case LBM_F64: return get_pops_t<double, float>(L, f);
+        case LBM_F16DEV: return get_pops_t<__half, float>(L, f);
+        default: return get_pops_t<__nv_bfloat16, float>(L, f);
+    }
+}
+
+int lbm_set_populations_f64(lbm_lattice* L, const double* f) {
+    if (int rc = check_handle(L)) return rc;
+    if (!f) return fail(LBM_ERR_INVALID_ARGUMENT, "null population pointer");
+    DeviceGuard g(L->dev);
+    L->mom_valid = false;
+    switch (L->precision) {
+        case LBM_F32: return set_pops_t<float, double>(L, f);
+        case LBM_F64: return set_pops_t<double, double>(L, f);
+        case LBM_F16DEV: return set_pops_t<__half, double>(L, f);
+        default: return set_pops_t<__nv_bfloat16, double>(L, f);
+    }
+}
+
+int lbm_get_populations_f64(lbm_lattice* L, double* f) {
+    if (int rc = check_handle(L)) return rc;
+    if (!f) return fail(LBM_ERR_INVALID_ARGUMENT, "null population pointer");
+    DeviceGuard g(L->dev);
+    switch (L->precision) {
+        case LBM_F32: return get_pops_t<float, double>(L, f);
+        case LBM_F64: return get_pops_t<double, double>(L, f);
+        case LBM_F16DEV: return get_pops_t<__half, double>(L, f);
+        default: return get_pops_t<__nv_bfloat16, double>(L, f);
+    }
+}
+
+int lbm_set_geometry(lbm_lattice* L, const uint8_t* solid) {
+    if (int rc = check_handle(L)) return rc;
+    DeviceGuard g(L->dev);
+    if (!solid) {
+        if (L->has_solid) { L->has_solid = false; L->dirty = true; }
+        return LBM_OK;
+    }
+    if (!L->solid) {
+        LBM_CUDA(cudaMalloc(reinterpret_cast<void**>(&L->solid), size_t(L->mpitch) * L->h));
+        LBM_CUDA(cudaMemsetAsync(L->solid, 0, size_t(L->mpitch) * L->h, L->stream));
+    }
+    LBM_CUDA(cudaMemcpy2DAsync(L->solid, L->mpitch, solid, L->w, L->w, L->h,
+                               cudaMemcpyHostToDevice, L->stream));
+    LBM_CUDA(cudaStreamSynchronize(L->stream));
+    if (!L->has_solid) { L->has_solid = true; L->dirty = true; }
+    return LBM_OK;
+}
+
+int lbm_set_force(lbm_lattice* L, float fx, float fy) {
+    if (int rc = check_handle(L)) return rc;
+    if (!std::isfinite(fx) || !std::isfinite(fy))
+        return fail(LBM_ERR_INVALID_ARGUMENT, "force must be finite");
+    L->fx = fx; L->fy = fy; L->dirty = true; L->mom_valid = false;
+    return LBM_OK;
+}
+
+int lbm_step(lbm_lattice* L, int nsteps) {
+    if (int rc = check_handle(L)) return rc;
+    DeviceGuard g(L->dev);
+    return steps_impl(L, nsteps, false);
+}
+
+int lbm_step_moments(lbm_lattice* L, int nsteps) {
+    if (int rc = check_handle(L)) return rc;
+    if (nsteps < 1) return fail(LBM_ERR_INVALID_ARGUMENT, "lbm_step_moments needs nsteps >= 1");
+    DeviceGuard g(L->dev);
+    return steps_impl(L, nsteps, true);
+}
+
+int lbm_read_moments(lbm_lattice* L, float* rho, float* ux, float* uy, int on_device) {
+    if (int rc = check_handle(L)) return rc;
+    if (!rho || !ux || !uy) return fail(LBM_ERR_INVALID_ARGUMENT, "null field pointer");
+    DeviceGuard g(L->dev);
+    if (!L->mom_valid) {
+        if (int rc = LBM_DISPATCH(L, moments_t, L)) return rc;
+        L->mom_valid = true;
+    }
+    float* dst[3] = {rho, ux, uy};
+    const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    for (int m = 0; m < 3; ++m)
+        LBM_CUDA(cudaMemcpy2DAsync(dst[m], size_t(L->w) * 4, L->mom[m], size_t(L->pitch) * 4,
+                                   size_t(L->w) * 4, L->h, kind, L->stream));
+    LBM_CUDA(cudaStreamSynchronize(L->stream));
+    return LBM_OK;
+}
+
+int lbm_check(lbm_lattice* L, lbm_health* out) {
+    if (int rc = check_handle(L)) return rc;
+    if (!out) return fail(LBM_ERR_INVALID_ARGUMENT, "null health pointer");
+    DeviceGuard g(L->dev);
+    if (int rc = LBM_DISPATCH(L, health_t, L)) return rc;
+    HealthPartial p;
+    LBM_CUDA(cudaMemcpyAsync(&p, L->health + kHealthBlocks, sizeof(p), cudaMemcpyDeviceToHost,
+                             L->stream));
+    LBM_CUDA(cudaStreamSynchronize(L->stream));
+    out->mass = p.mass;
+    out->momentum_x = p.mx;
+    out->momentum_y = p.my;
+    out->min_population = p.minf;
+    out->min_eq0 = p.mineq0;
+    out->nonfinite_count = p.nonfinite;
+    out->steps = L->steps;
+    out->unstable = (p.mineq0 < 0.0 || p.nonfinite > 0) ? 1 : 0;
+    out->reserved = 0;
+    return LBM_OK;
+}
+
+int lbm_get_time(lbm_lattice* L, float* time, int64_t* steps) {
+    if (int rc = check_handle(L)) return rc;
+    if (time) *time = L->time;
+    if (steps) *steps = L->steps;
+    return LBM_OK;
+}
+
+int lbm_set_stream(lbm_lattice* L, void* stream) {
+    if (int rc = check_handle(L)) return rc;
+    DeviceGuard g(L->dev);
+    LBM_CUDA(cudaStreamSynchronize(L->stream));
+    L->stream = stream ? static_cast<cudaStream_t>(stream) : L->own;
+    return LBM_OK;
+}
+
+int lbm_synchronize(lbm_lattice* L) {
+    if (int rc = check_handle(L)) return rc;
+    DeviceGuard g(L->dev);
+    LBM_CUDA(cudaStreamSynchronize(L->stream));
+    return LBM_OK;
+}
+
+int lbm_device_populations(lbm_lattice* L, void** base, int64_t* plane_stride, int* row_pitch) {
+    if (int rc = check_handle(L)) return rc;
+    if (base) *base = L->buf[L->cur];
+    if (plane_stride) *plane_stride = L->plane;
+    if (row_pitch) *row_pitch = L->pitch;
+    return LBM_OK;
+}
+
+int lbm_set_tile(lbm_lattice* L, int cells_per_thread, int rows_per_block) {
+    if (int rc = check_handle(L)) return rc;
+    const int v = cells_per_thread ? cells_per_thread : default_cells(L->precision);
+    const int r = rows_per_block ? rows_per_block : 4;
+    if (!valid_cells(L->precision, v))
+        return fail(LBM_ERR_INVALID_ARGUMENT, "cells_per_thread not available for this precision");
+    if (r < 1 || r > 8 || (L->h + r - 1) / r > 65535 || 32 * r > 256)
+        return fail(LBM_ERR_INVALID_ARGUMENT, "rows_per_block must be in [1, 8] and cover h");
+    L->vcells = v; L->rows = r; L->dirty = true;
+    return LBM_OK;
+}
+
+}  // extern "C"

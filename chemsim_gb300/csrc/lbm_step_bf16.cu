@@ -1,0 +1,15 @@
+// lbm_step_bf16.cu — fused-step launches for bfloat16 deviation storage.
+#include "lbm_step.cuh"
+
+namespace lbmk {
+
+template <>
+cudaError_t launch_step<__nv_bfloat16>(const StepArgs<float>& a, int frame, bool fast,
+                            int cells_per_thread, int rows, cudaStream_t stream) {
+    switch (cells_per_thread) {
+        case 8: return launch_step_v<__nv_bfloat16, 8>(a, frame, fast, rows, stream);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace lbmk

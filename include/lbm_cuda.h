@@ -1,0 +1,183 @@
+/*
+ * lbm_cuda.h — C ABI of the GB300 (sm_103a) D2Q9 lattice-Boltzmann solver.
+ *
+ * This is the drop-in boundary for taktoa/chemsim's `src/lbm.rs` lattice
+ * storage and `State::step`.  Every entry point is plain C: opaque handles,
+ * plain pointers and sizes, `int` status codes.  A Rust `lbm-cuda` crate binds
+ * these with `extern "C"` declarations (the binding is in INTEGRATION.md).
+ *
+ * Conventions
+ *  - Status: 0 = LBM_OK, negative = LBM_ERR_*.  The message of the last error
+ *    on the calling thread is returned by lbm_last_error_string().  The Rust
+ *    side turns a negative status into a panic, as lbm.rs does with
+ *    assert!/assert_eq! (src/lbm.rs:51-52,188,191; src/matrix.rs:26,33-36).
+ *  - Host field layout is row-major `y*w + x`, the layout of
+ *    `Matrix::new` / `Matrix::get_underlying` (src/matrix.rs:24-30,120-126):
+ *    row = y, column = x.
+ *  - Populations are structure-of-arrays: plane i (i = 0..8, the direction
+ *    order of `D2Q9::directions`, src/lbm.rs:202-282) occupies
+ *    f[i*w*h .. (i+1)*w*h), each plane row-major `y*w + x`.
+ *  - A handle owns its device memory and one CUDA stream.  A handle is not
+ *    thread-safe; separate handles are independent.
+ *  - Float precision of the device storage is chosen at creation; host
+ *    buffers are always f32 (f64 for the *_f64 entry points).
+ */
+#ifndef LBM_CUDA_H
+#define LBM_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define LBM_OK                    0
+#define LBM_ERR_INVALID_ARGUMENT (-1)
+#define LBM_ERR_OUT_OF_MEMORY    (-2)
+#define LBM_ERR_CUDA             (-3)
+#define LBM_ERR_UNSTABLE         (-4) /* health check found NaN/Inf or f_eq[0] < 0 */
+#define LBM_ERR_TIMEOUT          (-5) /* a bounded device-side wait expired       */
+#define LBM_ERR_NOT_SUPPORTED    (-6)
+#define LBM_ERR_STATE            (-7) /* call order violated (e.g. no data yet)  */
+
+/* ---- storage precision --------------------------------------------------- */
+#define LBM_F32      0 /* f32 populations (the reference's Scalar = f32, src/lbm.rs:13) */
+#define LBM_F64      1 /* f64 populations: the FP64 run of the same kernel             */
+#define LBM_F16DEV   2 /* IEEE half storing scaled (f_i - w_i), collided in f32        */
+#define LBM_BF16DEV  3 /* bfloat16 storing scaled (f_i - w_i), collided in f32         */
+
+/* ---- boundary / mode flags (OR them together) --------------------------- */
+/* Per-axis treatment of a pull source that lies outside the lattice.        */
+#define LBM_X_ZEROPAD   0x00 /* zeros enter (af::convolve2 DEFAULT, src/lbm.rs:722-724) */
+#define LBM_X_PERIODIC  0x01
+#define LBM_X_WALL      0x02 /* half-way bounce-back wall beyond x = -1/2 and w - 1/2 */
+#define LBM_Y_ZEROPAD   0x00
+#define LBM_Y_PERIODIC  0x04
+#define LBM_Y_WALL      0x08
+/* Solid-node treatment.                                                       */
+#define LBM_SOLID_FULLWAY 0x00 /* reference: after streaming, populations of a solid
+                                  node are reversed in place and the node collides
+                                  like any other (src/lbm.rs:741-751, :694-714)     */
+#define LBM_SOLID_HALFWAY 0x10 /* half-way bounce-back: a link whose source node is
+                                  solid returns the cell's own opposite population;
+                                  solid nodes keep their populations unchanged     */
+/* Frame: how a lattice velocity c = (cx, cy) maps to a grid displacement.     */
+#define LBM_FRAME_REF   0x00 /* lbm.rs: convolve2 with the transposed stencil moves
+                                direction i by (drow, dcol) = (-cx, +cy)           */
+#define LBM_FRAME_XY    0x20 /* c moves by (dcol, drow) = (+cx, +cy): x = column    */
+/* Arithmetic.                                                                   */
+#define LBM_FAST        0x40 /* FMA-contracted, algebraically simplified collision
+                                instead of the reference's operation order        */
+
+/* The exact lbm.rs semantics: zero-padded streaming, full-way bounce-back on
+ * solid nodes, the reference frame, the reference's f32 operation order.     */
+#define LBM_REFERENCE_FLAGS 0x00
+
+/* ---- collision operators ------------------------------------------------ */
+#define LBM_COLLISION_BGK 0 /* src/lbm.rs:345-370 */
+#define LBM_COLLISION_TRT 1 /* src/lbm.rs:374-451 */
+
+typedef struct lbm_lattice lbm_lattice;
+
+/* Global health of a lattice, reduced on the device in f64.
+ * Replaces State::is_unstable (src/lbm.rs:815-818) and Matrix::sum
+ * (src/matrix.rs:138-140) used as conservation checks.                        */
+typedef struct lbm_health {
+    double  mass;            /* sum of rho over all cells                        */
+    double  momentum_x;      /* sum of rho*u (lattice c-frame components)        */
+    double  momentum_y;
+    double  min_population;  /* min over cells and directions of f_i             */
+    double  min_eq0;         /* min over cells of f_eq[0]; < 0 is is_unstable()   */
+    int64_t nonfinite_count; /* populations that are NaN or +-Inf                */
+    int64_t steps;           /* steps taken since creation / last set            */
+    int32_t unstable;        /* 1 when min_eq0 < 0 or nonfinite_count > 0        */
+    int32_t reserved;
+} lbm_health;
+
+/* Returns the message of the last failed call on this thread ("" if none). */
+const char* lbm_last_error_string(void);
+
+/* Library version as MAJOR*10000 + MINOR*100 + PATCH. */
+int lbm_version(void);
+
+/* ---- single lattice ------------------------------------------------------ */
+
+/* Create a w x h lattice (1 <= w, h <= 262140).  Replaces D2Q9::new +
+ * State::initial (src/lbm.rs:187-200, :679-692).  Populations start at rest equilibrium
+ * (rho = 1, u = 0); time = 0; Discretization {dx = 1, dt = 1}; BGK(tau). */
+int lbm_create(int w, int h, float tau, int precision, int flags,
+               lbm_lattice** out);
+int lbm_destroy(lbm_lattice* lat);
+
+/* Discretization {delta_x, delta_t} (src/lbm.rs:75-86). */
+int lbm_set_discretization(lbm_lattice* lat, float delta_x, float delta_t);
+
+/* Collision operator: LBM_COLLISION_BGK uses tau (BGK { tau }, src/lbm.rs:345);
+ * LBM_COLLISION_TRT uses (tau_plus, tau_minus) (TRT, src/lbm.rs:374-377).   */
+int lbm_set_collision(lbm_lattice* lat, int kind, float tau, float tau_minus);
+
+/* Populations <- compute_equilibrium(rho, (ux, uy)) (src/lbm.rs:43-71).
+ * rho/ux/uy are host arrays of w*h floats, row-major y*w+x.               */
+int lbm_init_equilibrium(lbm_lattice* lat, const float* rho,
+                         const float* ux, const float* uy);
+
+/* Whole-state copies (9*w*h values, SoA, see layout above).  Replace
+ * Lattice::populations / populations_mut (src/lbm.rs:113-114).            */
+int lbm_set_populations(lbm_lattice* lat, const float* f);
+int lbm_get_populations(lbm_lattice* lat, float* f);
+int lbm_set_populations_f64(lbm_lattice* lat, const double* f);
+int lbm_get_populations_f64(lbm_lattice* lat, double* f);
+
+/* Solid mask (w*h bytes, nonzero = solid), replaces State::geometry
+ * (src/lbm.rs:99, :673).  Callable between steps, as LBMSim::handle does
+ * (src/main.rs:77-89).  NULL clears the geometry.                         */
+int lbm_set_geometry(lbm_lattice* lat, const uint8_t* solid);
+
+/* Constant body force (Guo forcing), in the lattice c-frame.  No reference
+ * counterpart (TODO.md:6 lists gravity as not done).                      */
+int lbm_set_force(lbm_lattice* lat, float fx, float fy);
+
+/* Advance nsteps time steps: stream -> bounce-back -> collide, time += dt
+ * (State::step, src/lbm.rs:694-714), one fused kernel per step, replayed
+ * from a CUDA graph.  Asynchronous on the handle's stream.               */
+int lbm_step(lbm_lattice* lat, int nsteps);
+
+/* As lbm_step; the last step also writes rho/u into the handle's device
+ * moment buffers, so a following lbm_read_moments costs only the copy.   */
+int lbm_step_moments(lbm_lattice* lat, int nsteps);
+
+/* rho, u of the current populations (Lattice::density / velocity,
+ * src/lbm.rs:117-149): rho = sum f_i, u = (1/rho) * sum f_i c_i (minus F/2
+ * when a force is set).  on_device != 0: the three pointers are device
+ * pointers.  Synchronises the handle's stream.                           */
+int lbm_read_moments(lbm_lattice* lat, float* rho, float* ux, float* uy,
+                     int on_device);
+
+/* Health check (see lbm_health).  Synchronises the handle's stream.      */
+int lbm_check(lbm_lattice* lat, lbm_health* out);
+
+/* State::time (src/lbm.rs:671) and the number of steps taken.            */
+int lbm_get_time(lbm_lattice* lat, float* time, int64_t* steps);
+
+/* Run the handle's work on a caller-provided CUDA stream (cudaStream_t
+ * passed as void*); NULL restores the handle's own stream.               */
+int lbm_set_stream(lbm_lattice* lat, void* stream);
+int lbm_synchronize(lbm_lattice* lat);
+
+/* Device pointer of population plane i of the current state, and the
+ * plane pitch in elements (for zero-copy consumers such as a renderer).   */
+int lbm_device_populations(lbm_lattice* lat, void** base, int64_t* plane_stride,
+                           int* row_pitch);
+
+/* Tile of the fused step: cells per thread along x (f32: 4 or 8; f64: 2;
+ * 16-bit: 8) and warps (rows) per block (1..8); 0 keeps the default.
+ * No reference counterpart (tuning knob of the GB300 kernel).            */
+int lbm_set_tile(lbm_lattice* lat, int cells_per_thread, int rows_per_block);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LBM_CUDA_H */

@@ -1,0 +1,379 @@
+"""CUDA path (through the C ABI) against the oracle — the parity tests.
+
+Bars: strict arithmetic (the reference's operation order) is bit-exact
+against the oracle in f32 and f64; LBM_FAST (FMA-contracted) stays within
+1e-5 relative per population in f32 (the tolerance the benchmark spec states for the
+f32 path) and 1e-12 in f64.
+"""
+import glob
+import math
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from chemsim_gb300 import lbm
+from chemsim_gb300.lbm import (BF16DEV, COLLISION_TRT, F16DEV, F32, F64, FAST, FRAME_XY,
+                               SOLID_HALFWAY, X_PERIODIC, X_WALL, Y_PERIODIC, Y_WALL, Lattice)
+from chemsim_gb300.workloads import channel_spec, taylor_green
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+FAST_RTOL = 1e-5
+
+
+def random_state(w, h, dtype, seed=0, du=0.05):
+    rng = np.random.default_rng(seed)
+    rho = (1 + rng.uniform(-0.01, 0.01, (h, w))).astype(dtype)
+    ux = rng.uniform(-du, du, (h, w)).astype(dtype)
+    uy = rng.uniform(-du, du, (h, w)).astype(dtype)
+    return oracle.equilibrium(rho, ux, uy)
+
+
+def gpu_run(f0, nsteps, *, tau, flags=0, precision=F32, solid=None, force=(0.0, 0.0),
+            collision=0, tau_minus=1.0, tile=None, out_dtype=None):
+    _, h, w = f0.shape
+    with Lattice(w, h, tau, precision, flags) as lat:
+        if collision:
+            lat.set_collision(collision, tau, tau_minus)
+        if force != (0.0, 0.0):
+            lat.set_force(*force)
+        if solid is not None:
+            lat.set_geometry(solid)
+        if tile:
+            lat.set_tile(*tile)
+        lat.set_populations(f0)
+        lat.step(nsteps)
+        f = lat.get_populations(out_dtype or f0.dtype)
+        return f, lat.moments(), lat.health(), lat.time()
+
+
+def assert_close_rel(a, b, rtol):
+    err = np.abs(a.astype(np.float64) - b.astype(np.float64))
+    bound = rtol * np.abs(b.astype(np.float64)) + 1e-30
+    worst = float(np.max(err / bound))
+    assert worst <= 1.0, f"max relative error {worst * rtol:.3e} > {rtol:.1e}"
+
+
+# -- the reference's own semantics (golden fixtures) ------------------------
+
+@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p) for p in GOLDEN])
+def test_golden_reference_mode_bit_exact(gpu, path):
+    g = np.load(path)
+    _, h, w = g["f0"].shape
+    with Lattice(w, h, float(g["tau"]), F32, lbm.REFERENCE_FLAGS) as lat:
+        lat.init_equilibrium(g["rho0"], g["ux0"], g["uy0"])
+        assert np.array_equal(lat.get_populations(), g["f0"])
+        if g["solid"].any():
+            lat.set_geometry(g["solid"])
+        lat.step(int(g["steps"]))
+        assert np.array_equal(lat.get_populations(), g["f"])
+        rho, ux, uy = lat.moments()
+        assert np.array_equal(rho, g["density"])
+        assert np.array_equal(ux, g["vx"])
+        assert np.array_equal(uy, g["vy"])
+
+
+def test_state_mirror_api(gpu):
+    g = np.load(GOLDEN[0])
+    pops = [g["f0"][i] for i in range(9)]
+    st = lbm.State.initial(lbm.D2Q9.new(pops), g["solid"].astype(bool),
+                           lbm.BGK(tau=float(g["tau"])), lbm.Discretization(1.0, 1.0))
+    for _ in range(int(g["steps"])):
+        st.step()
+    assert np.array_equal(st.populations(), g["f"])
+    assert np.array_equal(st.density(), g["density"])
+    vx, vy = st.velocity()
+    assert np.array_equal(vx, g["vx"]) and np.array_equal(vy, g["vy"])
+    assert st.time == np.float32(int(g["steps"]))
+    assert not st.is_unstable()
+    feq = st.equilibrium()
+    rho, ux, uy = oracle.moments(g["f"])
+    assert np.array_equal(feq, oracle.equilibrium(rho, ux, uy))
+    sp = st.speed()
+    np.testing.assert_allclose(sp, np.sqrt(vx * vx + vy * vy), rtol=1e-7)
+
+
+# -- every mode, size and tile: strict = bit-exact ------------------------
+
+MODES = [
+    0,
+    SOLID_HALFWAY,
+    X_PERIODIC | Y_PERIODIC,
+    X_PERIODIC | Y_PERIODIC | FRAME_XY,
+    X_PERIODIC | Y_WALL | SOLID_HALFWAY | FRAME_XY,
+    X_WALL | Y_WALL | SOLID_HALFWAY,
+    X_WALL | Y_PERIODIC | FRAME_XY,
+    X_PERIODIC | Y_WALL | SOLID_HALFWAY,
+]
+SIZES = [(1, 5), (3, 2), (5, 7), (31, 9), (32, 4), (33, 17), (129, 6), (130, 3), (200, 33)]
+
+
+@pytest.mark.parametrize("flags", MODES)
+@pytest.mark.parametrize("size", SIZES, ids=[f"{w}x{h}" for w, h in SIZES])
+def test_strict_f32_bit_exact(gpu, flags, size):
+    w, h = size
+    f0 = random_state(w, h, np.float32, seed=w * 100 + h)
+    solid = (np.random.default_rng(w + h).uniform(size=(h, w)) < 0.12).astype(np.uint8)
+    kw = dict(tau=0.7, flags=flags, solid=solid, force=(1e-5, -2e-5))
+    ref = oracle.step(f0, 7, **kw)
+    f, (rho, ux, uy), _, _ = gpu_run(f0, 7, **kw)
+    assert np.array_equal(f, ref)
+    r2, x2, y2 = oracle.moments(ref, force=kw["force"])
+    assert np.array_equal(rho, r2) and np.array_equal(ux, x2) and np.array_equal(uy, y2)
+
+
+@pytest.mark.parametrize("tile", [(4, 1), (4, 4), (4, 8), (8, 1), (8, 3), (8, 8)])
+@pytest.mark.parametrize("flags", [0, X_PERIODIC | Y_WALL | SOLID_HALFWAY | FRAME_XY,
+                                   X_PERIODIC | Y_PERIODIC])
+def test_strict_f32_tiles(gpu, tile, flags):
+    w, h = 301, 19
+    f0 = random_state(w, h, np.float32, seed=3)
+    solid = (np.random.default_rng(4).uniform(size=(h, w)) < 0.1).astype(np.uint8)
+    kw = dict(tau=0.66, flags=flags, solid=solid)
+    ref = oracle.step(f0, 5, **kw)
+    f, *_ = gpu_run(f0, 5, tile=tile, **kw)
+    assert np.array_equal(f, ref)
+
+
+@pytest.mark.parametrize("flags", MODES)
+@pytest.mark.parametrize("collision", [0, COLLISION_TRT])
+def test_strict_f64_bit_exact(gpu, flags, collision):
+    w, h = 37, 21
+    f0 = random_state(w, h, np.float64, seed=17)
+    solid = (np.random.default_rng(5).uniform(size=(h, w)) < 0.1).astype(np.uint8)
+    kw = dict(tau=0.62, flags=flags, solid=solid, force=(3e-6, 1e-6), collision=collision,
+              tau_minus=0.95)
+    ref = oracle.step(f0, 9, **kw)
+    f, *_ = gpu_run(f0, 9, precision=F64, **kw)
+    assert np.array_equal(f, ref)
+
+
+def test_trt_f32_bit_exact(gpu):
+    f0 = random_state(70, 40, np.float32, seed=21)
+    kw = dict(tau=0.8, tau_minus=1.2, collision=COLLISION_TRT, flags=X_PERIODIC | Y_PERIODIC)
+    ref = oracle.step(f0, 11, **kw)
+    f, *_ = gpu_run(f0, 11, **kw)
+    assert np.array_equal(f, ref)
+
+
+def test_graph_replay_path(gpu):
+    """Runs past the 64-step graph (two replays + a remainder) and matches."""
+    f0 = random_state(96, 40, np.float32, seed=6)
+    kw = dict(tau=0.9, flags=X_PERIODIC | Y_PERIODIC | FRAME_XY)
+    ref = oracle.step(f0, 131, **kw)
+    f, _, _, (t, n) = gpu_run(f0, 131, **kw)
+    assert np.array_equal(f, ref)
+    assert n == 131 and t == np.float32(131.0)
+
+
+def test_fast_f32_within_tolerance(gpu):
+    f0 = random_state(150, 64, np.float32, seed=8)
+    solid = (np.random.default_rng(1).uniform(size=(64, 150)) < 0.05).astype(np.uint8)
+    flags = X_PERIODIC | Y_WALL | SOLID_HALFWAY | FRAME_XY
+    kw = dict(tau=0.6, solid=solid, force=(1e-5, 0.0))
+    ref = oracle.step(f0, 200, flags=flags, **kw)
+    f, *_ = gpu_run(f0, 200, flags=flags | FAST, **kw)
+    assert_close_rel(f, ref, FAST_RTOL)
+
+
+def test_fast_f64_within_tolerance(gpu):
+    f0 = random_state(64, 48, np.float64, seed=9)
+    flags = X_PERIODIC | Y_PERIODIC | FRAME_XY
+    ref = oracle.step(f0, 100, tau=0.75, flags=flags)
+    f, *_ = gpu_run(f0, 100, tau=0.75, flags=flags | FAST, precision=F64)
+    assert_close_rel(f, ref, 1e-12)
+
+
+# -- the Taylor-Green lattice (256^2 periodic, tau = 0.8, 1000 steps) -------
+
+@pytest.fixture(scope="module")
+def taylor_green_1000():
+    rho, ux, uy = taylor_green(256, 256, u0=0.02, noise=1e-4, seed=1)
+    f0 = oracle.equilibrium(rho, ux, uy)
+    flags = X_PERIODIC | Y_PERIODIC | FRAME_XY
+    ref = oracle.step(f0, 1000, tau=0.8, flags=flags, threads=oracle.max_threads())
+    return f0, ref, flags
+
+
+def test_taylor_green_256_strict_bit_exact(gpu, taylor_green_1000):
+    f0, ref, flags = taylor_green_1000
+    f, _, health, _ = gpu_run(f0, 1000, tau=0.8, flags=flags)
+    assert np.array_equal(f, ref)
+    mass0 = float(np.sum(f0.astype(np.float64)))
+    assert abs(health["mass"] - mass0) / mass0 < 1e-6
+
+
+def test_taylor_green_256_fast_within_1e5(gpu, taylor_green_1000):
+    f0, ref, flags = taylor_green_1000
+    f, *_ = gpu_run(f0, 1000, tau=0.8, flags=flags | FAST)
+    assert_close_rel(f, ref, FAST_RTOL)
+
+
+@pytest.mark.parametrize("precision", [F32, F64])
+def test_taylor_green_viscosity(gpu, precision):
+    """Kinetic energy decays as exp(-4 nu k^2 t), nu = (tau - 1/2)/3."""
+    n, tau, steps = 128, 0.8, 2000
+    dtype = np.float64 if precision == F64 else np.float32
+    rho, ux, uy = taylor_green(n, n, u0=0.02, noise=0.0)
+    f0 = oracle.equilibrium(rho.astype(dtype), ux.astype(dtype), uy.astype(dtype))
+    flags = X_PERIODIC | Y_PERIODIC | FRAME_XY | FAST
+    _, (r, vx, vy), _, _ = gpu_run(f0, steps, tau=tau, flags=flags, precision=precision)
+    e0 = float(np.sum(ux.astype(np.float64) ** 2 + uy.astype(np.float64) ** 2))
+    e1 = float(np.sum(vx.astype(np.float64) ** 2 + vy.astype(np.float64) ** 2))
+    nu_fit = -math.log(e1 / e0) / (4 * (2 * math.pi / n) ** 2 * steps)
+    assert abs(nu_fit - (tau - 0.5) / 3) / ((tau - 0.5) / 3) < 0.005
+
+
+def test_mass_conserved_f64_periodic(gpu):
+    f0 = random_state(128, 96, np.float64, seed=12)
+    _, _, h, _ = gpu_run(f0, 500, tau=0.55, flags=X_PERIODIC | Y_PERIODIC | FAST, precision=F64)
+    h0 = oracle.health(f0)
+    assert abs(h["mass"] - h0["mass"]) / h0["mass"] < 1e-13
+    assert abs(h["momentum_x"] - h0["momentum_x"]) < 1e-11 * h0["mass"]
+    assert abs(h["momentum_y"] - h0["momentum_y"]) < 1e-11 * h0["mass"]
+
+
+# -- channel with obstacles and force ---------------------------------------
+
+def test_channel_strict_f32_bit_exact(gpu):
+    spec = channel_spec(384, n_obstacles=6, r_lo=8, r_hi=20, force=1e-5, h=256)
+    f0 = oracle.equilibrium(spec.rho, spec.ux, spec.uy)
+    kw = dict(tau=spec.tau, flags=spec.flags, solid=spec.solid, force=spec.force)
+    ref = oracle.step(f0, 40, threads=oracle.max_threads(), **kw)
+    f, *_ = gpu_run(f0, 40, **kw)
+    assert np.array_equal(f, ref)
+
+
+# -- deviation storage against the f64 run ----------------------------------
+
+def _l2(a, b):
+    a = a.astype(np.float64)
+    b = b.astype(np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+@pytest.mark.parametrize("precision,bound", [(F16DEV, 5e-3), (BF16DEV, 5e-2)])
+def test_deviation_storage_taylor_green(gpu, precision, bound):
+    n, steps = 128, 500
+    rho, ux, uy = taylor_green(n, n, u0=0.02, noise=1e-4)
+    flags = X_PERIODIC | Y_PERIODIC | FRAME_XY | FAST
+    res = {}
+    for p in (F64, precision):
+        with Lattice(n, n, 0.8, p, flags) as lat:
+            lat.init_equilibrium(rho, ux, uy)
+            lat.step(steps)
+            res[p] = lat.moments()
+    e_rho = _l2(res[precision][0] - 1.0, res[F64][0] - 1.0)
+    e_u = _l2(np.stack(res[precision][1:]), np.stack(res[F64][1:]))
+    print(f"precision {precision}: L2(rho-1) {e_rho:.3e}  L2(u) {e_u:.3e}")
+    assert e_u < bound
+
+
+def test_deviation_roundtrip(gpu):
+    f0 = random_state(40, 30, np.float32, seed=2)
+    for p, tol in [(F16DEV, 5e-5), (BF16DEV, 1e-3)]:
+        with Lattice(40, 30, 1.0, p, 0) as lat:
+            lat.set_populations(f0)
+            back = lat.get_populations()
+        assert np.max(np.abs(back - f0)) < tol
+
+
+# -- API behaviour -----------------------------------------------------------
+
+def test_step_moments_equal_readback(gpu):
+    f0 = random_state(77, 55, np.float32, seed=14)
+    flags = X_PERIODIC | Y_WALL | SOLID_HALFWAY | FRAME_XY
+    solid = (np.random.default_rng(2).uniform(size=(55, 77)) < 0.1).astype(np.uint8)
+    with Lattice(77, 55, 0.7, F32, flags) as a, Lattice(77, 55, 0.7, F32, flags) as b:
+        for lat in (a, b):
+            lat.set_force(2e-6, 0.0)
+            lat.set_geometry(solid)
+            lat.set_populations(f0)
+        a.step_moments(9)
+        b.step(9)
+        ma, mb = a.moments(), b.moments()
+        for x, y in zip(ma, mb):
+            assert np.array_equal(x, y)
+        assert np.array_equal(a.get_populations(), b.get_populations())
+
+
+def test_moments_to_device(gpu):
+    torch = pytest.importorskip("torch")
+    f0 = random_state(50, 20, np.float32, seed=3)
+    with Lattice(50, 20, 0.8, F32, X_PERIODIC | Y_PERIODIC) as lat:
+        lat.set_populations(f0)
+        lat.step(3)
+        host = lat.moments()
+        dev = [torch.empty((20, 50), dtype=torch.float32, device="cuda") for _ in range(3)]
+        lat.moments_to_device(*(t.data_ptr() for t in dev))
+        for hst, d in zip(host, dev):
+            assert np.array_equal(hst, d.cpu().numpy())
+
+
+def test_geometry_edit_between_steps(gpu):
+    """LBMSim::handle replaces the geometry between steps (src/main.rs:77-89)."""
+    w, h = 60, 40
+    f0 = random_state(w, h, np.float32, seed=30)
+    g1 = np.zeros((h, w), np.uint8)
+    g1[10:15, 10:15] = 1
+    g2 = np.zeros((h, w), np.uint8)
+    g2[20:30, 30:40] = 1
+    ref = oracle.step(f0, 5, tau=0.7, solid=g1)
+    ref = oracle.step(ref, 6, tau=0.7, solid=g2)
+    with Lattice(w, h, 0.7, F32, 0) as lat:
+        lat.set_populations(f0)
+        lat.set_geometry(g1)
+        lat.step(5)
+        lat.set_geometry(g2)
+        lat.step(6)
+        assert np.array_equal(lat.get_populations(), ref)
+        lat.set_geometry(None)
+        lat.step(2)
+        assert np.array_equal(lat.get_populations(), oracle.step(ref, 2, tau=0.7))
+
+
+def test_health_matches_oracle(gpu):
+    for dtype, prec in [(np.float32, F32), (np.float64, F64)]:
+        f0 = random_state(90, 70, dtype, seed=40)
+        with Lattice(90, 70, 0.8, prec, 0) as lat:
+            lat.set_populations(f0)
+            got = lat.health()
+        exp = oracle.health(f0)
+        assert abs(got["mass"] - exp["mass"]) < 1e-9
+        assert abs(got["momentum_x"] - exp["momentum_x"]) < 1e-9
+        assert abs(got["momentum_y"] - exp["momentum_y"]) < 1e-9
+        assert got["min_population"] == exp["min_population"]
+        assert got["min_eq0"] == exp["min_eq0"]
+        assert got["nonfinite_count"] == 0 and got["unstable"] == 0
+
+
+def test_health_flags_planted_nan_and_instability(gpu):
+    f0 = random_state(33, 17, np.float32, seed=41)
+    f0[2, 5, 7] = np.nan
+    with Lattice(33, 17, 0.8, F32, 0) as lat:
+        lat.set_populations(f0)
+        h = lat.health()
+    assert h["nonfinite_count"] == 1 and h["unstable"] == 1
+    g = random_state(33, 17, np.float32, seed=41)
+    g[1, 3, 3] += 5.0
+    with Lattice(33, 17, 0.8, F32, 0) as lat:
+        lat.set_populations(g)
+        h = lat.health()
+    assert h["min_eq0"] < 0 and h["unstable"] == 1 and h["nonfinite_count"] == 0
+
+
+def test_out_of_memory_is_a_status(gpu):
+    with pytest.raises(lbm.LBMError) as ei:
+        Lattice(262140, 262140, 0.8, F64, 0)
+    assert ei.value.status == lbm._lib.LBM_ERR_OUT_OF_MEMORY
+
+
+def test_bad_tile_rejected(gpu):
+    with Lattice(64, 64, 0.8, F32, 0) as lat:
+        with pytest.raises(lbm.LBMError):
+            lat.set_tile(3, 4)
+        with pytest.raises(lbm.LBMError):
+            lat.set_tile(4, 9)
