@@ -9,6 +9,7 @@
 #include <cstring>
 #include <string>
 #include <type_traits>
+#include <vector>
 
 #include "lbm_aux.cuh"
 
@@ -24,6 +25,7 @@ int fail(int code, const std::string& msg) {
 }
 
 int cuda_fail(cudaError_t e, const char* what) {
+    (void)cudaGetLastError();   // a non-sticky error must not leak into later calls
     return fail(e == cudaErrorMemoryAllocation ? LBM_ERR_OUT_OF_MEMORY : LBM_ERR_CUDA,
                 std::string(what) + ": " + cudaGetErrorString(e));
 }
@@ -61,9 +63,8 @@ size_t elem_size(int precision) {
 
 int default_cells(int precision) {
     switch (precision) {
-        case LBM_F32: return 4;
         case LBM_F64: return 2;
-        default: return 8;
+        default: return 4;
     }
 }
 
@@ -71,7 +72,7 @@ bool valid_cells(int precision, int v) {
     switch (precision) {
         case LBM_F32: return v == 4 || v == 8;
         case LBM_F64: return v == 2;
-        default: return v == 8;
+        default: return v == 4 || v == 8;
     }
 }
 
@@ -97,6 +98,11 @@ struct lbm_lattice {
     void* staging = nullptr;
     size_t staging_bytes = 0;
     HealthPartial* health = nullptr;      // kHealthBlocks partials + 1 result
+    uint8_t* tflags = nullptr;            // h x ceil(w / 32) bytes
+    int ntiles = 0;
+    uint32_t* gtiles = nullptr;           // list of flagged tiles
+    int ngtiles = 0;
+    size_t gtiles_cap = 0;
     int collision = LBM_COLLISION_BGK;
     float tau = 1.f, tau_minus = 1.f, dx = 1.f, dt = 1.f, fx = 0.f, fy = 0.f;
     float time = 0.f;
@@ -137,6 +143,12 @@ Consts<CT> make_consts(const lbm_lattice* L) {
     c.guo = CT(1) - CT(1) / (CT(2) * tau);
     c.inv_cs4 = CT(1) / cs4;
     c.force = (L->fx != 0.f || L->fy != 0.f) ? 1 : 0;
+    for (int i = 0; i < 9; ++i) {
+        const CT cF = CT(CX(i)) * c.fx + CT(CY(i)) * c.fy;
+        c.gw[i] = c.guo * c.wt[i];
+        c.kcF[i] = c.k1 * cF;
+        c.cF4[i] = cF * c.inv_cs4;
+    }
     c.collision = L->collision;
     if (L->precision == LBM_F16DEV) { c.dscale = CT(kHalfDevScale); c.dinv = CT(1) / CT(kHalfDevScale); }
     else if (L->precision == LBM_BF16DEV) { c.dscale = CT(kBf16DevScale); c.dinv = CT(1) / CT(kBf16DevScale); }
@@ -151,6 +163,10 @@ cudaError_t launch_one_t(lbm_lattice* L, int from, bool moments) {
     a.src = L->buf[from];
     a.dst = L->buf[from ^ 1];
     a.solid = L->has_solid ? L->solid : nullptr;
+    a.tflags = L->tflags;
+    a.ntiles = L->ntiles;
+    a.gtiles = L->gtiles;
+    a.ngtiles = L->ngtiles;
     if (moments) { a.mom_rho = L->mom[0]; a.mom_ux = L->mom[1]; a.mom_uy = L->mom[2]; }
     a.w = L->w; a.h = L->h; a.pitch = L->pitch; a.mpitch = L->mpitch; a.plane = L->plane;
     a.flags = L->flags;
@@ -202,6 +218,39 @@ int ensure_staging(lbm_lattice* L, size_t bytes) {
     L->staging_bytes = 0;
     LBM_CUDA(cudaMalloc(&L->staging, bytes));
     L->staging_bytes = bytes;
+    return LBM_OK;
+}
+
+// Recomputes the per-(row, warp tile) boundary/solid flags for the current
+// tile width and geometry.
+int refresh_tiles(lbm_lattice* L) {
+    const int tile_w = 32 * L->vcells;
+    L->ntiles = (L->w + tile_w - 1) / tile_w;
+    const int64_t n = int64_t(L->h) * L->ntiles;
+    tile_flags_kernel<<<grid_for(n, 256), 256, 0, L->stream>>>(
+        L->tflags, L->has_solid ? L->solid : nullptr, L->w, L->h, L->mpitch, tile_w, L->ntiles);
+    LBM_CUDA(cudaGetLastError());
+    // Compact the flagged tiles on the host (row-major order, deterministic).
+    std::vector<uint8_t> flags(static_cast<size_t>(n));
+    LBM_CUDA(cudaMemcpyAsync(flags.data(), L->tflags, flags.size(), cudaMemcpyDeviceToHost,
+                             L->stream));
+    LBM_CUDA(cudaStreamSynchronize(L->stream));
+    std::vector<uint32_t> list;
+    for (int64_t t = 0; t < n; ++t)
+        if (flags[size_t(t)]) list.push_back(uint32_t(t));
+    if (list.size() > L->gtiles_cap) {
+        if (L->gtiles) cudaFree(L->gtiles);
+        L->gtiles = nullptr;
+        L->gtiles_cap = 0;
+        LBM_CUDA(cudaMalloc(reinterpret_cast<void**>(&L->gtiles), list.size() * sizeof(uint32_t)));
+        L->gtiles_cap = list.size();
+    }
+    if (!list.empty())
+        LBM_CUDA(cudaMemcpyAsync(L->gtiles, list.data(), list.size() * sizeof(uint32_t),
+                                 cudaMemcpyHostToDevice, L->stream));
+    LBM_CUDA(cudaStreamSynchronize(L->stream));
+    L->ngtiles = int(list.size());
+    L->dirty = true;
     return LBM_OK;
 }
 
@@ -342,6 +391,35 @@ int steps_impl(lbm_lattice* L, int nsteps, bool moments) {
 }  // namespace
 
 namespace lbmk {
+__global__ void normalize_mask_kernel(uint8_t* __restrict__ m, int w, int h, int mpitch) {
+    const int64_t n = int64_t(w) * h;
+    for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < n;
+         t += int64_t(gridDim.x) * blockDim.x) {
+        const int y = int(t / w), x = int(t - int64_t(y) * w);
+        uint8_t* p = m + int64_t(y) * mpitch + x;
+        *p = *p != 0;
+    }
+}
+
+__global__ void tile_flags_kernel(uint8_t* __restrict__ tflags, const uint8_t* __restrict__ solid,
+                                  int w, int h, int mpitch, int tile_w, int ntiles) {
+    const int64_t n = int64_t(h) * ntiles;
+    for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < n;
+         t += int64_t(gridDim.x) * blockDim.x) {
+        const int y = int(t / ntiles), tt = int(t - int64_t(y) * ntiles);
+        const int xs = tt * tile_w;
+        bool gen = y == 0 || y == h - 1 || xs == 0 || xs + tile_w >= w;
+        if (!gen && solid != nullptr) {
+            for (int r = y - 1; r <= y + 1 && !gen; ++r) {
+                const uint8_t* row = solid + int64_t(r) * mpitch;
+                for (int c = xs - 1; c <= xs + tile_w; ++c)
+                    if (row[c]) { gen = true; break; }
+            }
+        }
+        tflags[t] = gen ? 1 : 0;
+    }
+}
+
 __global__ void health_final_kernel(const HealthPartial* __restrict__ partial, int nblocks,
                                     HealthPartial* __restrict__ out) {
     if (threadIdx.x != 0) return;
@@ -399,6 +477,8 @@ int lbm_create(int w, int h, float tau, int precision, int flags, lbm_lattice** 
     }
     e = cudaMalloc(reinterpret_cast<void**>(&L->health), sizeof(HealthPartial) * (kHealthBlocks + 1));
     if (e != cudaSuccess) return cleanup(cuda_fail(e, "health scratch"));
+    e = cudaMalloc(reinterpret_cast<void**>(&L->tflags), size_t(h) * ((w + 31) / 32));
+    if (e != cudaSuccess) return cleanup(cuda_fail(e, "tile flags"));
     e = cudaStreamCreateWithFlags(&L->own, cudaStreamNonBlocking);
     if (e != cudaSuccess) return cleanup(cuda_fail(e, "stream"));
     L->stream = L->own;
@@ -406,6 +486,7 @@ int lbm_create(int w, int h, float tau, int precision, int flags, lbm_lattice** 
         int rc = LBM_DISPATCH(L, fill_rest_t, L, b);
         if (rc) return cleanup(rc);
     }
+    if (int rc = refresh_tiles(L)) return cleanup(rc);
     e = cudaStreamSynchronize(L->stream);
     if (e != cudaSuccess) return cleanup(cuda_fail(e, "create"));
     *out = L;
@@ -423,6 +504,8 @@ int lbm_destroy(lbm_lattice* L) {
         if (L->solid) cudaFree(L->solid);
         if (L->staging) cudaFree(L->staging);
         if (L->health) cudaFree(L->health);
+        if (L->tflags) cudaFree(L->tflags);
+        if (L->gtiles) cudaFree(L->gtiles);
         if (L->own) cudaStreamDestroy(L->own);
     }
     delete L;
@@ -519,7 +602,11 @@ int lbm_set_geometry(lbm_lattice* L, const uint8_t* solid) {
     if (int rc = check_handle(L)) return rc;
     DeviceGuard g(L->dev);
     if (!solid) {
-        if (L->has_solid) { L->has_solid = false; L->dirty = true; }
+        if (L->has_solid) {
+            L->has_solid = false;
+            if (int rc = refresh_tiles(L)) return rc;
+            LBM_CUDA(cudaStreamSynchronize(L->stream));
+        }
         return LBM_OK;
     }
     if (!L->solid) {
@@ -528,8 +615,12 @@ int lbm_set_geometry(lbm_lattice* L, const uint8_t* solid) {
     }
     LBM_CUDA(cudaMemcpy2DAsync(L->solid, L->mpitch, solid, L->w, L->w, L->h,
                                cudaMemcpyHostToDevice, L->stream));
+    normalize_mask_kernel<<<grid_for(int64_t(L->w) * L->h, 256), 256, 0, L->stream>>>(
+        L->solid, L->w, L->h, L->mpitch);
+    LBM_CUDA(cudaGetLastError());
+    L->has_solid = true;
+    if (int rc = refresh_tiles(L)) return rc;
     LBM_CUDA(cudaStreamSynchronize(L->stream));
-    if (!L->has_solid) { L->has_solid = true; L->dirty = true; }
     return LBM_OK;
 }
 
@@ -630,7 +721,10 @@ int lbm_set_tile(lbm_lattice* L, int cells_per_thread, int rows_per_block) {
         return fail(LBM_ERR_INVALID_ARGUMENT, "cells_per_thread not available for this precision");
     if (r < 1 || r > 8 || (L->h + r - 1) / r > 65535 || 32 * r > 256)
         return fail(LBM_ERR_INVALID_ARGUMENT, "rows_per_block must be in [1, 8] and cover h");
+    DeviceGuard g(L->dev);
     L->vcells = v; L->rows = r; L->dirty = true;
+    if (int rc = refresh_tiles(L)) return rc;
+    LBM_CUDA(cudaStreamSynchronize(L->stream));
     return LBM_OK;
 }
 

@@ -115,6 +115,16 @@ __global__ void moments_kernel(const S* __restrict__ f, float* __restrict__ rho,
     }
 }
 
+// Solid-mask bytes -> exactly 0 or 1 (the step kernel packs them with a
+// multiply that needs 0/1 bytes).
+__global__ void normalize_mask_kernel(uint8_t* __restrict__ m, int w, int h, int mpitch);
+
+// Per (row, warp tile of tile_w cells): 1 when the tile touches a lattice
+// edge row/column or has a solid cell within one cell of it, 0 otherwise
+// (interior tiles take the step kernel's lean path).
+__global__ void tile_flags_kernel(uint8_t* __restrict__ tflags, const uint8_t* __restrict__ solid,
+                                  int w, int h, int mpitch, int tile_w, int ntiles);
+
 struct HealthPartial {
     double mass, mx, my, minf, mineq0;
     long long nonfinite;

@@ -37,38 +37,75 @@ static_assert(OPP(5) == 7 && OPP(6) == 8 && OPP(7) == 5 && OPP(8) == 6, "opp");
 // Storage traits: S is the stored element type, CT the collision type.
 // Deviation storage keeps (f_i - w_i) * scale in 16 bits.
 template <class S> struct Store;
-template <> struct Store<float> {
-    using CT = float;
+// Plain storage: decode / encode are the identity.
+template <class T>
+struct PlainStore {
+    using CT = T;
     static constexpr bool DEV = false;
-    __device__ static float dec(float s, float, float) { return s; }
-    __device__ static float enc(float f, float, float) { return f; }
+    __device__ static T dec(T s, T, T) { return s; }
+    __device__ static T enc(T f, T, T) { return f; }
+    template <int V>
+    __device__ static void dec_vec(const T (&s)[V], T (&f)[V], T, T) {
+#pragma unroll
+        for (int k = 0; k < V; ++k) f[k] = s[k];
+    }
+    template <int V>
+    __device__ static void enc_vec(const T (&f)[V], T (&s)[V], T, T) {
+#pragma unroll
+        for (int k = 0; k < V; ++k) s[k] = f[k];
+    }
 };
-template <> struct Store<double> {
-    using CT = double;
-    static constexpr bool DEV = false;
-    __device__ static double dec(double s, double, double) { return s; }
-    __device__ static double enc(double f, double, double) { return f; }
-};
-template <> struct Store<__half> {
+template <> struct Store<float> : PlainStore<float> {};
+template <> struct Store<double> : PlainStore<double> {};
+// 16-bit deviation storage; the vector forms convert element pairs with one
+// paired conversion instruction.
+template <class H, class H2>
+struct DevStore {
     using CT = float;
     static constexpr bool DEV = true;
-    __device__ static float dec(__half s, float w, float inv_scale) {
-        return __fmaf_rn(__half2float(s), inv_scale, w);
+    __device__ static float to_f(H s);
+    __device__ static H from_f(float f);
+    __device__ static float2 to_f2(H2 s);
+    __device__ static H2 from_f2(float2 f);
+    __device__ static float dec(H s, float w, float inv_scale) {
+        return __fmaf_rn(to_f(s), inv_scale, w);
     }
-    __device__ static __half enc(float f, float w, float scale) {
-        return __float2half_rn(__fmul_rn(__fsub_rn(f, w), scale));
+    __device__ static H enc(float f, float w, float scale) {
+        return from_f(__fmul_rn(__fsub_rn(f, w), scale));
+    }
+    template <int V>
+    __device__ static void dec_vec(const H (&s)[V], float (&f)[V], float w, float inv_scale) {
+        static_assert(V % 2 == 0, "pairs");
+#pragma unroll
+        for (int k = 0; k < V; k += 2) {
+            H2 p;
+            memcpy(&p, &s[k], sizeof(H2));
+            const float2 q = to_f2(p);
+            f[k] = __fmaf_rn(q.x, inv_scale, w);
+            f[k + 1] = __fmaf_rn(q.y, inv_scale, w);
+        }
+    }
+    template <int V>
+    __device__ static void enc_vec(const float (&f)[V], H (&s)[V], float w, float scale) {
+        static_assert(V % 2 == 0, "pairs");
+#pragma unroll
+        for (int k = 0; k < V; k += 2) {
+            const H2 p = from_f2(make_float2(__fmul_rn(__fsub_rn(f[k], w), scale),
+                                             __fmul_rn(__fsub_rn(f[k + 1], w), scale)));
+            memcpy(&s[k], &p, sizeof(H2));
+        }
     }
 };
-template <> struct Store<__nv_bfloat16> {
-    using CT = float;
-    static constexpr bool DEV = true;
-    __device__ static float dec(__nv_bfloat16 s, float w, float inv_scale) {
-        return __fmaf_rn(__bfloat162float(s), inv_scale, w);
-    }
-    __device__ static __nv_bfloat16 enc(float f, float w, float scale) {
-        return __float2bfloat16_rn(__fmul_rn(__fsub_rn(f, w), scale));
-    }
-};
+template <> __device__ inline float DevStore<__half, __half2>::to_f(__half s) { return __half2float(s); }
+template <> __device__ inline __half DevStore<__half, __half2>::from_f(float f) { return __float2half_rn(f); }
+template <> __device__ inline float2 DevStore<__half, __half2>::to_f2(__half2 s) { return __half22float2(s); }
+template <> __device__ inline __half2 DevStore<__half, __half2>::from_f2(float2 f) { return __float22half2_rn(f); }
+template <> __device__ inline float DevStore<__nv_bfloat16, __nv_bfloat162>::to_f(__nv_bfloat16 s) { return __bfloat162float(s); }
+template <> __device__ inline __nv_bfloat16 DevStore<__nv_bfloat16, __nv_bfloat162>::from_f(float f) { return __float2bfloat16_rn(f); }
+template <> __device__ inline float2 DevStore<__nv_bfloat16, __nv_bfloat162>::to_f2(__nv_bfloat162 s) { return __bfloat1622float2(s); }
+template <> __device__ inline __nv_bfloat162 DevStore<__nv_bfloat16, __nv_bfloat162>::from_f2(float2 f) { return __float22bfloat162_rn(f); }
+template <> struct Store<__half> : DevStore<__half, __half2> {};
+template <> struct Store<__nv_bfloat16> : DevStore<__nv_bfloat16, __nv_bfloat162> {};
 
 // Power-of-two scale of the deviation formats: keeps |f_i - w_i| >= 1e-8
 // out of the half subnormal range while |f_i - w_i| <= 7 still fits.
@@ -88,6 +125,9 @@ struct Consts {
     CT guo;                 // 1 - 1/(2 tau)
     CT inv_cs4;
     CT dscale, dinv;        // deviation-storage scale and its inverse
+    CT gw[9];               // guo * w_i                      (fast path)
+    CT kcF[9];              // k1 * (c_i . F)                 (fast path)
+    CT cF4[9];              // (c_i . F) / cs^4               (fast path)
     int collision;          // LBM_COLLISION_*
     int force;              // nonzero when a body force is set
 };
@@ -98,6 +138,10 @@ struct StepArgs {
     const void* src;        // 9 planes, current state
     void* dst;              // 9 planes, next state
     const uint8_t* solid;   // mask (pitch mpitch) or null
+    const uint8_t* tflags;  // per (row, warp tile): 1 = boundary/solid nearby, or null
+    int ntiles;             // warp tiles per row (row stride of tflags)
+    const uint32_t* gtiles; // flagged tiles (row * ntiles + tile), or null
+    int ngtiles;
     float* mom_rho;         // moment outputs (pitch `pitch`) or null
     float* mom_ux;
     float* mom_uy;

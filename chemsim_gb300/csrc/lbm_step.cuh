@@ -13,6 +13,13 @@
 // realigned in registers with warp shuffles, so every global load is an
 // aligned, coalesced vector; only the two lanes at a warp's ends fetch one
 // extra scalar (an L1/L2 hit).  Row shifts are plain row offsets.
+//
+// Each step is two launches: the interior kernel over every (row, warp tile)
+// whose 3 x (32V + 2) neighbourhood is inside the lattice and fluid (a lean
+// path with no boundary logic), and the general kernel over the list of
+// remaining tiles (lattice edges, solids), which carries the full boundary
+// treatment.  The per-tile flags are rebuilt whenever the geometry or the
+// tile width changes.
 #pragma once
 
 #include "lbm_common.cuh"
@@ -63,61 +70,53 @@ struct VecIO {
     }
 };
 
+// V solid bits (bit k <-> column xl + k) from V mask bytes that hold exactly
+// 0 or 1: the multiply gathers byte k's low bit into bit 28 + k (every
+// partial product lands on its own bit, so no carries interfere).
 template <int V>
 __device__ __forceinline__ uint32_t load_mask_core(const uint8_t* p) {
-    uint32_t bits = 0;
+    constexpr uint32_t M = 0x10204080u;
     if constexpr (V == 8) {
         const uint2 r = __ldg(reinterpret_cast<const uint2*>(p));
-#pragma unroll
-        for (int k = 0; k < 4; ++k) bits |= (((r.x >> (8 * k)) & 0xffu) != 0u) << k;
-#pragma unroll
-        for (int k = 0; k < 4; ++k) bits |= (((r.y >> (8 * k)) & 0xffu) != 0u) << (k + 4);
+        return ((r.x * M) >> 28) | (((r.y * M) >> 28) << 4);
     } else if constexpr (V == 4) {
-        const unsigned r = __ldg(reinterpret_cast<const unsigned*>(p));
-#pragma unroll
-        for (int k = 0; k < 4; ++k) bits |= (((r >> (8 * k)) & 0xffu) != 0u) << k;
+        return (__ldg(reinterpret_cast<const unsigned*>(p)) * M) >> 28;
     } else if constexpr (V == 2) {
-        const unsigned short r = __ldg(reinterpret_cast<const unsigned short*>(p));
-        bits = ((r & 0xffu) != 0u) | ((((r >> 8) & 0xffu) != 0u) << 1);
+        return (uint32_t(__ldg(reinterpret_cast<const unsigned short*>(p))) * M) >> 28;
     } else {
-        bits = __ldg(p) != 0;
+        return __ldg(p);
     }
-    return bits;
 }
 
 // Solid bit of column col of a mask row, with the x-axis rule for columns
 // outside [0, w): wrapped when periodic, 0 otherwise (the axis rule decides).
 __device__ __forceinline__ uint32_t mask_at(const uint8_t* row, int col, int w, bool xper) {
-    if (col >= 0 && col < w) return __ldg(row + col) != 0;
+    if (col >= 0 && col < w) return __ldg(row + col);
     if (xper) {
         int c = col % w;
         if (c < 0) c += w;
-        return __ldg(row + c) != 0;
+        return __ldg(row + c);
     }
     return 0;
 }
 
-// Bits j = 0..V+1 <-> solid(column x0 - 1 + j) of one mask row.
-template <int V>
-__device__ __forceinline__ uint32_t mask_row_bits(const uint8_t* row, int x0, int xl,
-                                                  int w, int lane, bool xper) {
-    uint32_t core = load_mask_core<V>(row + xl);
-    uint32_t left = __shfl_up_sync(kFull, (core >> (V - 1)) & 1u, 1);
-    uint32_t right = __shfl_down_sync(kFull, core & 1u, 1);
-    if (lane == 0 || x0 == 0) left = mask_at(row, x0 - 1, w, xper);
-    if (lane == 31 || x0 + V >= w) {
-        right = mask_at(row, x0 + V, w, xper);
-#pragma unroll
-        for (int k = 0; k < V; ++k)
-            if (x0 + k >= w) core = (core & ~(1u << k)) | (mask_at(row, x0 + k, w, xper) << k);
+// Source row of a direction with row displacement dr; *cls = 0 (cells),
+// 1 (zero-padded) or 2 (bounce-back wall) when the row lies outside.
+__device__ __forceinline__ int source_row(int y, int dr, int h, int ym, int* cls) {
+    int sr = y - dr;
+    *cls = 0;
+    if (sr < 0 || sr >= h) {
+        if (ym == 1) sr = sr < 0 ? sr + h : sr - h;
+        else { *cls = (ym == 2) ? 2 : 1; sr = 0; }
     }
-    return left | (core << 1) | (right << (V + 1));
+    return sr;
 }
 
-// The collision of one cell: f (pre-collision, post-streaming) -> out.
-template <bool FAST, class CT>
-__device__ __forceinline__ void collide_cell(const Consts<CT>& c, const CT (&f)[9], CT (&out)[9]) {
-    using A = Ar<FAST>;
+// Collision of one cell in the reference's operation order (strict).
+template <class CT>
+__device__ __forceinline__ void collide_strict(const Consts<CT>& c, const CT (&f)[9],
+                                               CT (&out)[9]) {
+    using A = Ar<false>;
     // density (src/lbm.rs:117-121) and momentum_density (:123-131); the terms
     // f_i * 0 and the +-1 products are exact, so the nonzero terms are summed
     // in the reference's order.
@@ -157,16 +156,9 @@ __device__ __forceinline__ void collide_cell(const Consts<CT>& c, const CT (&f)[
 #pragma unroll
     for (int i = 0; i < 9; ++i) {
         const CT rw = i == 0 ? rw0 : (i < 5 ? rw1 : rw5);
-        CT s;
-        if constexpr (FAST) {
-            s = fma(vc[i], c.k1, CT(1));
-            s = fma(vc[i] * vc[i], c.k2, s);
-            s = s + v2k3;
-        } else {
-            s = A::add(CT(1), A::mul(vc[i], c.k1));
-            s = A::add(s, A::mul(A::mul(vc[i], vc[i]), c.k2));
-            s = A::add(s, v2k3);
-        }
+        CT s = A::add(CT(1), A::mul(vc[i], c.k1));
+        s = A::add(s, A::mul(A::mul(vc[i], vc[i]), c.k2));
+        s = A::add(s, v2k3);
         feq[i] = A::mul(rw, s);
     }
     if (c.collision == LBM_COLLISION_TRT) {
@@ -188,10 +180,7 @@ __device__ __forceinline__ void collide_cell(const Consts<CT>& c, const CT (&f)[
         }
     } else {
 #pragma unroll
-        for (int i = 0; i < 9; ++i) {
-            if constexpr (FAST) out[i] = fma(f[i] - feq[i], c.bgk_factor, f[i]);
-            else out[i] = A::add(f[i], A::mul(A::sub(f[i], feq[i]), c.bgk_factor));
-        }
+        for (int i = 0; i < 9; ++i) out[i] = A::add(f[i], A::mul(A::sub(f[i], feq[i]), c.bgk_factor));
     }
     if (c.force) {
 #pragma unroll
@@ -206,6 +195,71 @@ __device__ __forceinline__ void collide_cell(const Consts<CT>& c, const CT (&f)[
             out[i] = A::add(out[i], A::mul(wg, A::add(t1, t2)));
         }
     }
+}
+
+// The same collision with contracted, regrouped arithmetic: opposite
+// directions share |c.u| so f_eq of a pair is A +- B, and the Guo term uses
+// the precomputed c_i . F.
+template <class CT>
+__device__ __forceinline__ void collide_fast(const Consts<CT>& c, const CT (&f)[9],
+                                             CT (&out)[9]) {
+    const CT rho = ((f[0] + f[1]) + (f[2] + f[3])) + ((f[4] + f[5]) + (f[6] + f[7])) + f[8];
+    CT mx = (f[1] - f[3]) + (f[5] - f[6]) + (f[8] - f[7]);
+    CT my = (f[2] - f[4]) + (f[5] + f[6]) - (f[7] + f[8]);
+    if (c.force) { mx += c.hfx; my += c.hfy; }
+    const CT inv = Ar<true>::rcp(rho);
+    const CT ux = mx * inv, uy = my * inv;
+    const CT base = fma(fma(ux, ux, uy * uy), c.k3, CT(1));
+    const CT rw0 = rho * c.wt[0], rw1 = rho * c.wt[1], rw5 = rho * c.wt[5];
+    const CT rk1 = rw1 * c.k1, rk5 = rw5 * c.k1;
+    CT feq[9];
+    feq[0] = rw0 * base;
+    {
+        const CT A = rw1 * fma(c.k2, ux * ux, base), B = rk1 * ux;
+        feq[1] = A + B; feq[3] = A - B;
+    }
+    {
+        const CT A = rw1 * fma(c.k2, uy * uy, base), B = rk1 * uy;
+        feq[2] = A + B; feq[4] = A - B;
+    }
+    const CT d = ux + uy, e = uy - ux;
+    {
+        const CT A = rw5 * fma(c.k2, d * d, base), B = rk5 * d;
+        feq[5] = A + B; feq[7] = A - B;
+    }
+    {
+        const CT A = rw5 * fma(c.k2, e * e, base), B = rk5 * e;
+        feq[6] = A + B; feq[8] = A - B;
+    }
+    if (c.collision == LBM_COLLISION_TRT) {
+#pragma unroll
+        for (int i = 0; i < 9; ++i) {
+            const CT fsw = f[OPP(i)];
+            const CT eqsw = (i == 0) ? feq[0] : fsw;
+            const CT om = ((f[i] + fsw) - (feq[i] + eqsw)) * c.omega_p +
+                          ((f[i] - fsw) - (feq[i] - eqsw)) * c.omega_m;
+            out[i] = fma(om, c.trt_scale, f[i]);
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < 9; ++i) out[i] = fma(f[i] - feq[i], c.bgk_factor, f[i]);
+    }
+    if (c.force) {
+        // S_i = guo w_i (k1 (c_i.F - u.F) + (c_i.u)(c_i.F)/cs^4)
+        const CT uF = c.k1 * fma(ux, c.fx, uy * c.fy);
+        CT vc[9];
+        vc[0] = CT(0); vc[1] = ux; vc[2] = uy; vc[3] = -ux; vc[4] = -uy;
+        vc[5] = d; vc[6] = e; vc[7] = -d; vc[8] = -e;
+#pragma unroll
+        for (int i = 0; i < 9; ++i)
+            out[i] = fma(c.gw[i], fma(vc[i], c.cF4[i], c.kcF[i] - uF), out[i]);
+    }
+}
+
+template <bool FAST, class CT>
+__device__ __forceinline__ void collide_cell(const Consts<CT>& c, const CT (&f)[9], CT (&out)[9]) {
+    if constexpr (FAST) collide_fast<CT>(c, f, out);
+    else collide_strict<CT>(c, f, out);
 }
 
 // Moments of a stored cell state (Lattice::density / velocity, src/lbm.rs:
@@ -233,31 +287,130 @@ __device__ __forceinline__ void cell_moments(const Consts<CT>& c, const CT (&f)[
     uy = A::mul(inv, my);
 }
 
+// Writes the V collided cells of a thread and, when requested, their moments
+// (computed from the stored, i.e. encoded, values).
+template <class S, int V, bool FAST>
+__device__ __forceinline__ void store_cells(const StepArgs<typename Store<S>::CT>& a, int y,
+                                            int x0, const S (&enc)[9][V]) {
+    using CT = typename Store<S>::CT;
+    using ST = Store<S>;
+    S* __restrict__ dst = static_cast<S*>(a.dst);
+    const int64_t PL = a.plane;
+    const int w = a.w;
+    const int64_t base = int64_t(y) * a.pitch + x0;
+    if (x0 + V <= w) {
+#pragma unroll
+        for (int i = 0; i < 9; ++i) VecIO<S, V>::store(dst + i * PL + base, enc[i]);
+    } else {
+#pragma unroll
+        for (int i = 0; i < 9; ++i)
+#pragma unroll
+            for (int k = 0; k < V; ++k)
+                if (x0 + k < w) dst[i * PL + base + k] = enc[i][k];
+    }
+    if (a.mom_rho != nullptr) {
+#pragma unroll
+        for (int k = 0; k < V; ++k) {
+            if (x0 + k >= w) break;
+            CT g[9];
+#pragma unroll
+            for (int i = 0; i < 9; ++i) g[i] = ST::dec(enc[i][k], a.c.wt[i], a.c.dinv);
+            CT r, ux, uy;
+            cell_moments<FAST>(a.c, g, r, ux, uy);
+            a.mom_rho[base + k] = float(r);
+            a.mom_ux[base + k] = float(ux);
+            a.mom_uy[base + k] = float(uy);
+        }
+    }
+}
+
+// Interior warp tile: every source cell is inside the lattice and fluid (the
+// tile flags say so), so a step is 9 vector loads, 6 shuffles and two edge
+// scalars per lane, the collision and 9 vector stores.
 template <class S, int V, int FRAME, bool FAST>
-__global__ void __launch_bounds__(256)
-lbm_step_kernel(const StepArgs<typename Store<S>::CT> a) {
+__device__ __forceinline__ void step_interior(const StepArgs<typename Store<S>::CT>& a, int y,
+                                              int x0, int lane) {
+    using CT = typename Store<S>::CT;
+    using ST = Store<S>;
+    const S* __restrict__ base = static_cast<const S*>(a.src) + int64_t(y) * a.pitch + x0;
+    const int64_t P = a.pitch, PL = a.plane;
+    S raw[9][V];
+    S edge[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+        const int dc = DCOL(FRAME, i), dr = DROW(FRAME, i);
+        const S* p = base + i * PL - dr * P;
+        VecIO<S, V>::load(p, raw[i]);
+        edge[i] = raw[i][0];
+        if (dc == 1 && lane == 0) edge[i] = __ldg(p - 1);
+        if (dc == -1 && lane == 31) edge[i] = __ldg(p + V);
+    }
+    CT f[9][V];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+        const int dc = DCOL(FRAME, i);
+        const CT wi = a.c.wt[i];
+        CT v[V];
+        ST::dec_vec(raw[i], v, wi, a.c.dinv);
+        if (dc == 1) {
+            const CT left = __shfl_up_sync(kFull, v[V - 1], 1);
+#pragma unroll
+            for (int k = V - 1; k > 0; --k) v[k] = v[k - 1];
+            v[0] = lane == 0 ? ST::dec(edge[i], wi, a.c.dinv) : left;
+        } else if (dc == -1) {
+            const CT right = __shfl_down_sync(kFull, v[0], 1);
+#pragma unroll
+            for (int k = 0; k < V - 1; ++k) v[k] = v[k + 1];
+            v[V - 1] = lane == 31 ? ST::dec(edge[i], wi, a.c.dinv) : right;
+        }
+#pragma unroll
+        for (int k = 0; k < V; ++k) f[i][k] = v[k];
+    }
+#pragma unroll
+    for (int k = 0; k < V; ++k) {
+        CT g[9], o[9];
+#pragma unroll
+        for (int i = 0; i < 9; ++i) g[i] = f[i][k];
+        collide_cell<FAST>(a.c, g, o);
+#pragma unroll
+        for (int i = 0; i < 9; ++i) f[i][k] = o[i];
+    }
+    S enc[9][V];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) ST::enc_vec(f[i], enc[i], a.c.wt[i], a.c.dscale);
+    store_cells<S, V, FAST>(a, y, x0, enc);
+}
+
+// One time step of one lattice.  Phase A issues every global load of the
+// thread (3 mask rows, 9 population vectors and the warp-edge scalars) before
+// any of them is consumed, so a thread has ~150 B in flight and pays one
+// memory latency; phase B realigns the +-1 column shifts with shuffles and
+// classifies boundary links; phase C fetches the cell's own opposite
+// populations for bounce-back links (only near walls and solids); phase D
+// collides and stores.
+template <class S, int V, int FRAME, bool FAST>
+__device__ __forceinline__ void step_general(const StepArgs<typename Store<S>::CT>& a, int y,
+                                             int tile, int lane) {
     using CT = typename Store<S>::CT;
     using ST = Store<S>;
     using IO = VecIO<S, V>;
     constexpr uint32_t FULL = (1u << V) - 1u;
 
-    const int lane = threadIdx.x;
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
-    if (y >= a.h) return;                       // warp-uniform
     const int w = a.w, h = a.h;
-    const int x0 = (blockIdx.x * 32 + lane) * V;
+    const int x0 = (tile * 32 + lane) * V;
     const bool active = x0 < w;
     const int xl = active ? x0 : 0;            // idle lanes read a valid chunk
     const S* __restrict__ src = static_cast<const S*>(a.src);
-    S* __restrict__ dst = static_cast<S*>(a.dst);
     const int64_t P = a.pitch, PL = a.plane;
     const int xm = a.flags & 3, ym = (a.flags >> 2) & 3;
     const bool halfway = (a.flags & LBM_SOLID_HALFWAY) != 0;
     const bool has_solid = a.solid != nullptr;
     const bool xper = xm == 1;
+    const bool left_edge = lane == 0 || x0 == 0;          // needs column x0 - 1 itself
+    const bool right_edge = lane == 31 || x0 + V >= w;    // needs column x0 + V itself
 
-    // Solid bits of rows y-1, y, y+1 (index 1 - drow of a direction).
-    uint32_t mrow[3] = {0u, 0u, 0u};
+    // ---- phase A: issue all loads ----------------------------------------
+    uint32_t mcore[3] = {0u, 0u, 0u}, mleft[3] = {0u, 0u, 0u}, mright[3] = {0u, 0u, 0u};
     if (has_solid) {
 #pragma unroll
         for (int r = 0; r < 3; ++r) {
@@ -267,8 +420,54 @@ lbm_step_kernel(const StepArgs<typename Store<S>::CT> a) {
                 if (ym == 1) row = row < 0 ? row + h : row - h;
                 else ok = false;
             }
-            if (ok)   // warp-uniform
-                mrow[r] = mask_row_bits<V>(a.solid + int64_t(row) * a.mpitch, x0, xl, w, lane, xper);
+            if (ok) {   // warp-uniform
+                const uint8_t* mr = a.solid + int64_t(row) * a.mpitch;
+                mcore[r] = load_mask_core<V>(mr + xl);
+                if (left_edge) mleft[r] = mask_at(mr, x0 - 1, w, xper);
+                if (right_edge) mright[r] = mask_at(mr, x0 + V, w, xper);
+            }
+        }
+    }
+
+    S raw[9][V];
+    S edge[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+        const int dc = DCOL(FRAME, i), dr = DROW(FRAME, i);
+        int cls;
+        const int sr = source_row(y, dr, h, ym, &cls);
+        const S* prow = src + i * PL + int64_t(sr) * P;
+        IO::load(prow + xl, raw[i]);
+        edge[i] = raw[i][0];
+        if (dc == 1) {
+            int ec = x0 - 1;
+            if (ec < 0) ec = xper ? w - 1 : -1;
+            if (left_edge && ec >= 0) edge[i] = __ldg(prow + ec);
+        } else if (dc == -1) {
+            int ec = x0 + V;
+            if (ec >= w) ec = (xper && ec == w) ? 0 : -1;
+            if (right_edge && ec >= 0) edge[i] = __ldg(prow + ec);
+        }
+    }
+
+    // ---- phase B: realign, classify ---------------------------------------
+    uint32_t mrow[3] = {0u, 0u, 0u};
+    if (has_solid) {
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            uint32_t core = mcore[r];
+            const uint32_t l = __shfl_up_sync(kFull, (core >> (V - 1)) & 1u, 1);
+            const uint32_t rr = __shfl_down_sync(kFull, core & 1u, 1);
+            if (x0 + V > w && xper) {            // partial last chunk, periodic: wrap
+                int row = y - 1 + r;
+                if (row < 0) row += h;
+                if (row >= h) row -= h;
+                const uint8_t* mr = a.solid + int64_t(row) * a.mpitch;
+#pragma unroll
+                for (int k = 0; k < V; ++k)
+                    if (x0 + k >= w) core = (core & ~(1u << k)) | (mask_at(mr, x0 + k, w, true) << k);
+            }
+            mrow[r] = (left_edge ? mleft[r] : l) | (core << 1) | ((right_edge ? mright[r] : rr) << (V + 1));
         }
     }
 
@@ -277,71 +476,64 @@ lbm_step_kernel(const StepArgs<typename Store<S>::CT> a) {
 #pragma unroll
     for (int i = 0; i < 9; ++i) {
         const int dc = DCOL(FRAME, i), dr = DROW(FRAME, i);
-        int sr = y - dr;
-        int rowcls = 0;                          // 0 cells, 1 zero, 2 bounce
-        if (sr < 0 || sr >= h) {
-            if (ym == 1) sr = sr < 0 ? sr + h : sr - h;
-            else rowcls = (ym == 2) ? 2 : 1;
-        }
-        const S* plane = src + i * PL;
-        const S* prow = plane + int64_t(rowcls == 0 ? sr : 0) * P;
         const CT wi = a.c.wt[i];
         CT v[V];
-        {
-            S raw[V];
-            IO::load(prow + xl, raw);
-#pragma unroll
-            for (int k = 0; k < V; ++k) v[k] = ST::dec(raw[k], wi, a.c.dinv);
-        }
+        ST::dec_vec(raw[i], v, wi, a.c.dinv);
+        const CT e = ST::dec(edge[i], wi, a.c.dinv);
         uint32_t xz = 0u, xb = 0u;
         if (dc == 1) {
             const CT left = __shfl_up_sync(kFull, v[V - 1], 1);
 #pragma unroll
             for (int k = V - 1; k > 0; --k) v[k] = v[k - 1];
-            v[0] = left;
-            if (lane == 0 || x0 == 0) {
-                int sx = x0 - 1;
-                if (sx >= 0) v[0] = ST::dec(__ldg(prow + sx), wi, a.c.dinv);
-                else if (xper) v[0] = ST::dec(__ldg(prow + sx + w), wi, a.c.dinv);
-                else if (xm == 2) xb |= 1u;
-                else xz |= 1u;
-            }
+            v[0] = left_edge ? e : left;
+            if (x0 == 0 && !xper) { if (xm == 2) xb |= 1u; else xz |= 1u; }
         } else if (dc == -1) {
             const CT right = __shfl_down_sync(kFull, v[0], 1);
 #pragma unroll
             for (int k = 0; k < V - 1; ++k) v[k] = v[k + 1];
-            v[V - 1] = right;
-            if (lane == 31 || x0 + V >= w) {
+            v[V - 1] = right_edge ? e : right;
+            if (x0 + V >= w) {                   // the row's last chunk (rare)
+                int cls;
+                const S* prow = src + i * PL + int64_t(source_row(y, dr, h, ym, &cls)) * P;
 #pragma unroll
                 for (int k = 0; k < V; ++k) {
                     const int sx = x0 + k + 1;
                     if (sx >= w) {
-                        if (xper) v[k] = ST::dec(__ldg(prow + (sx % w)), wi, a.c.dinv);
-                        else if (xm == 2) xb |= 1u << k;
-                        else xz |= 1u << k;
-                    } else if (k == V - 1) {
-                        v[k] = ST::dec(__ldg(prow + sx), wi, a.c.dinv);
+                        if (xper) {
+                            if (!(k == V - 1 && sx == w))   // not already the edge load
+                                v[k] = ST::dec(__ldg(prow + (sx % w)), wi, a.c.dinv);
+                        } else if (xm == 2) {
+                            xb |= 1u << k;
+                        } else {
+                            xz |= 1u << k;
+                        }
                     }
                 }
             }
         }
-        uint32_t b = (rowcls == 2) ? FULL : xb;
-        const uint32_t z = (rowcls == 1 ? FULL : xz) & ~b;
+        int cls;
+        (void)source_row(y, dr, h, ym, &cls);
+        uint32_t b = (cls == 2) ? FULL : xb;
+        const uint32_t z = (cls == 1 ? FULL : xz) & ~b;
         if (has_solid && halfway) b |= (mrow[1 - dr] >> (1 - dc)) & FULL;
+        if (z) {
 #pragma unroll
-        for (int k = 0; k < V; ++k) f[i][k] = ((z >> k) & 1u) ? CT(0) : v[k];
+            for (int k = 0; k < V; ++k) if ((z >> k) & 1u) v[k] = CT(0);
+        }
+#pragma unroll
+        for (int k = 0; k < V; ++k) f[i][k] = v[k];
         bnc[i] = b;
     }
 
-    // Bounce-back links: the cell's own post-collision opposite population.
+    // ---- phase C: bounce-back links take the cell's own opposite population
 #pragma unroll
     for (int i = 1; i < 9; ++i) {
         if (bnc[i]) {
-            S raw[V];
-            IO::load(src + OPP(i) * PL + int64_t(y) * P + xl, raw);
+            S own[V];
+            IO::load(src + OPP(i) * PL + int64_t(y) * P + xl, own);
 #pragma unroll
             for (int k = 0; k < V; ++k)
-                if ((bnc[i] >> k) & 1u) f[i][k] = ST::dec(raw[k], a.c.wt[OPP(i)], a.c.dinv);
+                if ((bnc[i] >> k) & 1u) f[i][k] = ST::dec(own[k], a.c.wt[OPP(i)], a.c.dinv);
         }
     }
 
@@ -360,8 +552,8 @@ lbm_step_kernel(const StepArgs<typename Store<S>::CT> a) {
         }
     }
 
-    // Collide and write.
-    CT out[9][V];
+    // ---- phase D: collide and write ---------------------------------------
+    S enc[9][V];
 #pragma unroll
     for (int k = 0; k < V; ++k) {
         CT g[9], o[9];
@@ -369,66 +561,87 @@ lbm_step_kernel(const StepArgs<typename Store<S>::CT> a) {
         for (int i = 0; i < 9; ++i) g[i] = f[i][k];
         collide_cell<FAST>(a.c, g, o);
 #pragma unroll
-        for (int i = 0; i < 9; ++i) out[i][k] = o[i];
+        for (int i = 0; i < 9; ++i) f[i][k] = o[i];
     }
-    S enc[9][V];
 #pragma unroll
-    for (int i = 0; i < 9; ++i)
-#pragma unroll
-        for (int k = 0; k < V; ++k) enc[i][k] = ST::enc(out[i][k], a.c.wt[i], a.c.dscale);
+    for (int i = 0; i < 9; ++i) ST::enc_vec(f[i], enc[i], a.c.wt[i], a.c.dscale);
 
     if (own_solid && halfway) {
         // Half-way mode: solid nodes keep their populations.
 #pragma unroll
         for (int i = 0; i < 9; ++i) {
-            S raw[V];
-            IO::load(src + i * PL + int64_t(y) * P + xl, raw);
+            S own[V];
+            IO::load(src + i * PL + int64_t(y) * P + xl, own);
 #pragma unroll
             for (int k = 0; k < V; ++k)
-                if ((own_solid >> k) & 1u) enc[i][k] = raw[k];
+                if ((own_solid >> k) & 1u) enc[i][k] = own[k];
         }
     }
 
     if (!active) return;
-    const int64_t base = int64_t(y) * P + x0;
-    if (x0 + V <= w) {
-#pragma unroll
-        for (int i = 0; i < 9; ++i) IO::store(dst + i * PL + base, enc[i]);
-    } else {
-#pragma unroll
-        for (int i = 0; i < 9; ++i)
-#pragma unroll
-            for (int k = 0; k < V; ++k)
-                if (x0 + k < w) dst[i * PL + base + k] = enc[i][k];
-    }
+    store_cells<S, V, FAST>(a, y, x0, enc);
+}
 
-    if (a.mom_rho != nullptr) {
-#pragma unroll
-        for (int k = 0; k < V; ++k) {
-            if (x0 + k >= w) break;
-            CT g[9];
-#pragma unroll
-            for (int i = 0; i < 9; ++i) g[i] = ST::dec(enc[i][k], a.c.wt[i], a.c.dinv);
-            CT r, ux, uy;
-            cell_moments<FAST>(a.c, g, r, ux, uy);
-            a.mom_rho[base + k] = float(r);
-            a.mom_ux[base + k] = float(ux);
-            a.mom_uy[base + k] = float(uy);
-        }
+// Interior tiles of the whole lattice: grid (tiles per row, rows / warps per
+// block); a warp whose tile is flagged leaves at once (the general kernel
+// owns it).
+template <class S, int V, int FRAME, bool FAST>
+__global__ void __launch_bounds__(256, (sizeof(typename Store<S>::CT) == 4 && V <= 4) ? 3 : 1)
+lbm_interior_kernel(const StepArgs<typename Store<S>::CT> a) {
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (y >= a.h) return;
+    if (a.tflags[int64_t(y) * a.ntiles + blockIdx.x] != 0) return;     // warp-uniform
+    step_interior<S, V, FRAME, FAST>(a, y, (blockIdx.x * 32 + threadIdx.x) * V, threadIdx.x);
+}
+
+// The flagged tiles (a lattice edge or a solid within one cell), one warp per
+// entry of the list a.gtiles (entry = row * ntiles + tile); with no list,
+// every tile of the lattice (grid as the interior kernel's).
+template <class S, int V, int FRAME, bool FAST>
+__global__ void __launch_bounds__(256)
+lbm_step_kernel(const StepArgs<typename Store<S>::CT> a) {
+    int y, tile;
+    if (a.gtiles != nullptr) {
+        const int e = blockIdx.x * blockDim.y + threadIdx.y;
+        if (e >= a.ngtiles) return;
+        const uint32_t t = a.gtiles[e];
+        y = int(t / uint32_t(a.ntiles));
+        tile = int(t - uint32_t(y) * uint32_t(a.ntiles));
+    } else {
+        y = blockIdx.y * blockDim.y + threadIdx.y;
+        if (y >= a.h) return;
+        tile = blockIdx.x;
+    }
+    step_general<S, V, FRAME, FAST>(a, y, tile, threadIdx.x);
+}
+
+template <class S, int V, int FRAME, bool FAST>
+void launch_step_tv(const StepArgs<typename Store<S>::CT>& a, int rows, cudaStream_t stream) {
+    const dim3 block(32, rows);
+    const dim3 full((a.w + 32 * V - 1) / (32 * V), (a.h + rows - 1) / rows);
+    if (a.tflags != nullptr) {
+        lbm_interior_kernel<S, V, FRAME, FAST><<<full, block, 0, stream>>>(a);
+        if (a.ngtiles > 0)
+            lbm_step_kernel<S, V, FRAME, FAST><<<(a.ngtiles + rows - 1) / rows, block, 0, stream>>>(a);
+    } else {
+        StepArgs<typename Store<S>::CT> b = a;
+        b.gtiles = nullptr;
+        lbm_step_kernel<S, V, FRAME, FAST><<<full, block, 0, stream>>>(b);
     }
 }
 
+// One step: the interior kernel plus the general kernel over the flagged
+// tiles (with tile flags), or the general kernel over every tile (without).
 template <class S, int V>
 cudaError_t launch_step_v(const StepArgs<typename Store<S>::CT>& a, int frame, bool fast,
                           int rows, cudaStream_t stream) {
-    const dim3 block(32, rows);
-    const dim3 grid((a.w + 32 * V - 1) / (32 * V), (a.h + rows - 1) / rows);
+    (void)cudaGetLastError();   // report this launch's status, not an earlier call's
     if (frame) {
-        if (fast) lbm_step_kernel<S, V, 1, true><<<grid, block, 0, stream>>>(a);
-        else lbm_step_kernel<S, V, 1, false><<<grid, block, 0, stream>>>(a);
+        if (fast) launch_step_tv<S, V, 1, true>(a, rows, stream);
+        else launch_step_tv<S, V, 1, false>(a, rows, stream);
     } else {
-        if (fast) lbm_step_kernel<S, V, 0, true><<<grid, block, 0, stream>>>(a);
-        else lbm_step_kernel<S, V, 0, false><<<grid, block, 0, stream>>>(a);
+        if (fast) launch_step_tv<S, V, 0, true>(a, rows, stream);
+        else launch_step_tv<S, V, 0, false>(a, rows, stream);
     }
     return cudaGetLastError();
 }

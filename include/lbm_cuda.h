@@ -172,7 +172,7 @@ int lbm_device_populations(lbm_lattice* lat, void** base, int64_t* plane_stride,
                            int* row_pitch);
 
 /* Tile of the fused step: cells per thread along x (f32: 4 or 8; f64: 2;
- * 16-bit: 8) and warps (rows) per block (1..8); 0 keeps the default.
+ * 16-bit: 4 or 8) and warps (rows) per block (1..8); 0 keeps the default.
  * No reference counterpart (tuning knob of the GB300 kernel).            */
 int lbm_set_tile(lbm_lattice* lat, int cells_per_thread, int rows_per_block);
 
