@@ -95,6 +95,8 @@ SIGNATURES = {
     "lbm_device_populations": (_i32, [_vp, ctypes.POINTER(_vp), ctypes.POINTER(_i64),
                                       ctypes.POINTER(_i32)]),
     "lbm_set_tile": (_i32, [_vp, _i32, _i32]),
+    "lbm_check_device_noalloc": (_i32, [_vp, _i32, _i32, _i32, _i32, _i64, _f32, _f32, _vp,
+                                        ctypes.POINTER(LBMHealth)]),
 }
 
 _lock = threading.Lock()

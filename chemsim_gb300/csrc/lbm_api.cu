@@ -391,6 +391,8 @@ int steps_impl(lbm_lattice* L, int nsteps, bool moments) {
 }  // namespace
 
 namespace lbmk {
+void set_last_error(const std::string& msg) { g_err = msg; }
+
 __global__ void normalize_mask_kernel(uint8_t* __restrict__ m, int w, int h, int mpitch) {
     const int64_t n = int64_t(w) * h;
     for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < n;

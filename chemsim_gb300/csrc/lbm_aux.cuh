@@ -6,6 +6,8 @@
 
 #include <math.h>
 
+#include <string>
+
 #include "lbm_step.cuh"
 
 namespace lbmk {
@@ -124,6 +126,9 @@ __global__ void normalize_mask_kernel(uint8_t* __restrict__ m, int w, int h, int
 // (interior tiles take the step kernel's lean path).
 __global__ void tile_flags_kernel(uint8_t* __restrict__ tflags, const uint8_t* __restrict__ solid,
                                   int w, int h, int mpitch, int tile_w, int ntiles);
+
+// Sets the message lbm_last_error_string returns on this thread.
+void set_last_error(const std::string& msg);
 
 struct HealthPartial {
     double mass, mx, my, minf, mineq0;

@@ -171,6 +171,26 @@ int lbm_synchronize(lbm_lattice* lat);
 int lbm_device_populations(lbm_lattice* lat, void** base, int64_t* plane_stride,
                            int* row_pitch);
 
+/* Health check (as lbm_check) of populations the caller already holds on the
+ * device, for callers that cannot call cudaMalloc: render or game loops that
+ * must not pay cudaMalloc's implicit device synchronisation, hosts that have
+ * reserved all device memory for their own pool, plugin hosts that forbid
+ * library allocations.  No counterpart in the reference.
+ *   populations: plane 0 of 9 SoA planes of the given precision, rows of
+ *   row_pitch elements, planes plane_stride elements apart (the layout
+ *   lbm_device_populations returns); stream: cudaStream_t or NULL.
+ * Allocates nothing: its scratch is a static 768 KiB device array that every
+ * GPU loading this library holds until exit.  At most 268435456 cells
+ * (16384 x 16384); larger lattices return LBM_ERR_INVALID_ARGUMENT.  The
+ * first call on a device resolves the array's device address (make that
+ * first call before any stream capture).  Calls share the array, so calls
+ * that overlap on the GPU race; every call overwrites all of the scratch it
+ * reads, so nothing needs clearing between calls.  Synchronises `stream`;
+ * out->steps is 0.                                                          */
+int lbm_check_device_noalloc(const void* populations, int precision, int w, int h,
+                             int row_pitch, int64_t plane_stride, float delta_x,
+                             float delta_t, void* stream, lbm_health* out);
+
 /* Tile of the fused step: cells per thread along x (f32: 4 or 8; f64: 2;
  * 16-bit: 4 or 8) and warps (rows) per block (1..8); 0 keeps the default.
  * No reference counterpart (tuning knob of the GB300 kernel).            */
