@@ -153,6 +153,9 @@ Consts<CT> make_consts(const lbm_lattice* L) {
     if (L->precision == LBM_F16DEV) { c.dscale = CT(kHalfDevScale); c.dinv = CT(1) / CT(kHalfDevScale); }
     else if (L->precision == LBM_BF16DEV) { c.dscale = CT(kBf16DevScale); c.dinv = CT(1) / CT(kBf16DevScale); }
     else { c.dscale = CT(1); c.dinv = CT(1); }
+    for (int i = 0; i < 9; ++i) c.sgw[i] = c.dscale * c.gw[i];
+    c.shfx = c.dscale * c.hfx;
+    c.shfy = c.dscale * c.hfy;
     return c;
 }
 
@@ -227,8 +230,12 @@ int refresh_tiles(lbm_lattice* L) {
     const int tile_w = 32 * L->vcells;
     L->ntiles = (L->w + tile_w - 1) / tile_w;
     const int64_t n = int64_t(L->h) * L->ntiles;
+    // Edge tiles of a periodic-x row whose width is a whole number of tiles
+    // only need wrapped edge addresses: the interior kernel takes them.
+    const int xwrap = ((L->flags & 3) == LBM_X_PERIODIC && L->w % tile_w == 0) ? 1 : 0;
     tile_flags_kernel<<<grid_for(n, 256), 256, 0, L->stream>>>(
-        L->tflags, L->has_solid ? L->solid : nullptr, L->w, L->h, L->mpitch, tile_w, L->ntiles);
+        L->tflags, L->has_solid ? L->solid : nullptr, L->w, L->h, L->mpitch, tile_w, L->ntiles,
+        xwrap);
     LBM_CUDA(cudaGetLastError());
     // Compact the flagged tiles on the host (row-major order, deterministic).
     std::vector<uint8_t> flags(static_cast<size_t>(n));
@@ -237,7 +244,7 @@ int refresh_tiles(lbm_lattice* L) {
     LBM_CUDA(cudaStreamSynchronize(L->stream));
     std::vector<uint32_t> list;
     for (int64_t t = 0; t < n; ++t)
-        if (flags[size_t(t)]) list.push_back(uint32_t(t));
+        if (flags[size_t(t)] == 1) list.push_back(uint32_t(t));
     if (list.size() > L->gtiles_cap) {
         if (L->gtiles) cudaFree(L->gtiles);
         L->gtiles = nullptr;
@@ -404,21 +411,24 @@ __global__ void normalize_mask_kernel(uint8_t* __restrict__ m, int w, int h, int
 }
 
 __global__ void tile_flags_kernel(uint8_t* __restrict__ tflags, const uint8_t* __restrict__ solid,
-                                  int w, int h, int mpitch, int tile_w, int ntiles) {
+                                  int w, int h, int mpitch, int tile_w, int ntiles, int xwrap) {
     const int64_t n = int64_t(h) * ntiles;
     for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < n;
          t += int64_t(gridDim.x) * blockDim.x) {
         const int y = int(t / ntiles), tt = int(t - int64_t(y) * ntiles);
         const int xs = tt * tile_w;
-        bool gen = y == 0 || y == h - 1 || xs == 0 || xs + tile_w >= w;
+        const bool xedge = xs == 0 || xs + tile_w >= w;
+        bool gen = y == 0 || y == h - 1 || (xedge && !xwrap);
         if (!gen && solid != nullptr) {
             for (int r = y - 1; r <= y + 1 && !gen; ++r) {
                 const uint8_t* row = solid + int64_t(r) * mpitch;
-                for (int c = xs - 1; c <= xs + tile_w; ++c)
-                    if (row[c]) { gen = true; break; }
+                for (int c = xs - 1; c <= xs + tile_w; ++c) {
+                    const int cc = c < 0 ? c + w : (c >= w ? c - w : c);
+                    if (row[cc]) { gen = true; break; }
+                }
             }
         }
-        tflags[t] = gen ? 1 : 0;
+        tflags[t] = gen ? 1 : (xedge ? 2 : 0);
     }
 }
 

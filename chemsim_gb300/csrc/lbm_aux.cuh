@@ -122,10 +122,11 @@ __global__ void moments_kernel(const S* __restrict__ f, float* __restrict__ rho,
 __global__ void normalize_mask_kernel(uint8_t* __restrict__ m, int w, int h, int mpitch);
 
 // Per (row, warp tile of tile_w cells): 1 when the tile touches a lattice
-// edge row/column or has a solid cell within one cell of it, 0 otherwise
-// (interior tiles take the step kernel's lean path).
+// edge row, a non-wrapping edge column or has a solid cell within one cell of
+// it; 2 for an edge tile of a wrapping (periodic, whole tiles) row; 0
+// otherwise.  Tiles flagged 0 or 2 take the interior kernel.
 __global__ void tile_flags_kernel(uint8_t* __restrict__ tflags, const uint8_t* __restrict__ solid,
-                                  int w, int h, int mpitch, int tile_w, int ntiles);
+                                  int w, int h, int mpitch, int tile_w, int ntiles, int xwrap);
 
 // Sets the message lbm_last_error_string returns on this thread.
 void set_last_error(const std::string& msg);

@@ -54,6 +54,19 @@ struct PlainStore {
 #pragma unroll
         for (int k = 0; k < V; ++k) s[k] = f[k];
     }
+    // The step kernels' working variables ("domain"): f itself.
+    __device__ static T dec_dom(T s) { return s; }
+    __device__ static T zero_dom(T, T) { return T(0); }
+    template <int V>
+    __device__ static void dec_vec_dom(const T (&s)[V], T (&f)[V]) {
+#pragma unroll
+        for (int k = 0; k < V; ++k) f[k] = s[k];
+    }
+    template <int V>
+    __device__ static void enc_vec_dom(const T (&f)[V], T (&s)[V]) {
+#pragma unroll
+        for (int k = 0; k < V; ++k) s[k] = f[k];
+    }
 };
 template <> struct Store<float> : PlainStore<float> {};
 template <> struct Store<double> : PlainStore<double> {};
@@ -95,6 +108,29 @@ struct DevStore {
             memcpy(&s[k], &p, sizeof(H2));
         }
     }
+    // The step kernels' working variables ("domain"): the scaled deviation
+    // G_i = s (f_i - w_i) itself, so loading and storing are bare conversions.
+    __device__ static float dec_dom(H s) { return to_f(s); }
+    __device__ static float zero_dom(float w, float scale) { return -w * scale; }   // f = 0
+    template <int V>
+    __device__ static void dec_vec_dom(const H (&s)[V], float (&f)[V]) {
+#pragma unroll
+        for (int k = 0; k < V; k += 2) {
+            H2 p;
+            memcpy(&p, &s[k], sizeof(H2));
+            const float2 q = to_f2(p);
+            f[k] = q.x;
+            f[k + 1] = q.y;
+        }
+    }
+    template <int V>
+    __device__ static void enc_vec_dom(const float (&f)[V], H (&s)[V]) {
+#pragma unroll
+        for (int k = 0; k < V; k += 2) {
+            const H2 p = from_f2(make_float2(f[k], f[k + 1]));
+            memcpy(&s[k], &p, sizeof(H2));
+        }
+    }
 };
 template <> __device__ inline float DevStore<__half, __half2>::to_f(__half s) { return __half2float(s); }
 template <> __device__ inline __half DevStore<__half, __half2>::from_f(float f) { return __float2half_rn(f); }
@@ -128,6 +164,8 @@ struct Consts {
     CT gw[9];               // guo * w_i                      (fast path)
     CT kcF[9];              // k1 * (c_i . F)                 (fast path)
     CT cF4[9];              // (c_i . F) / cs^4               (fast path)
+    CT sgw[9];              // dscale * guo * w_i             (deviation form)
+    CT shfx, shfy;          // dscale * F / 2                 (deviation form)
     int collision;          // LBM_COLLISION_*
     int force;              // nonzero when a body force is set
 };

@@ -14,11 +14,11 @@
 // aligned, coalesced vector; only the two lanes at a warp's ends fetch one
 // extra scalar (an L1/L2 hit).  Row shifts are plain row offsets.
 //
-// Each step is two launches: the interior kernel over every (row, warp tile)
-// whose 3 x (32V + 2) neighbourhood is inside the lattice and fluid (a lean
-// path with no boundary logic), and the general kernel over the list of
-// remaining tiles (lattice edges, solids), which carries the full boundary
-// treatment.  The per-tile flags are rebuilt whenever the geometry or the
+// Each step is one launch with two paths: the interior path for every
+// (row, warp tile) whose 3 x (32V + 2) neighbourhood is inside the lattice and
+// fluid (no boundary logic at all), and the general path, with the full
+// boundary treatment, for the listed remaining tiles (lattice edges, solids).
+// The per-tile flags and the list are rebuilt whenever the geometry or the
 // tile width changes.
 #pragma once
 
@@ -262,6 +262,66 @@ __device__ __forceinline__ void collide_cell(const Consts<CT>& c, const CT (&f)[
     else collide_strict<CT>(c, f, out);
 }
 
+// The same collision in the scaled deviation variables of 16-bit storage,
+// G_i = s (f_i - w_i):  rho = 1 + sum(G)/s,  u = sum(G c)/(s + sum(G)),
+// G_eq_i = w_i (sum(G) + (s + sum(G)) P_i) with P_i = k1 c.u + k2 (c.u)^2
+// + k3 u^2, and BGK / Guo are linear in G.  No offset by w_i is ever added or
+// removed, so loads and stores are bare format conversions.
+template <class CT>
+__device__ __forceinline__ void collide_dev(const Consts<CT>& c, const CT (&G)[9], CT (&out)[9]) {
+    const CT DR = ((G[0] + G[1]) + (G[2] + G[3])) + ((G[4] + G[5]) + (G[6] + G[7])) + G[8];
+    CT jx = (G[1] - G[3]) + (G[5] - G[6]) + (G[8] - G[7]);
+    CT jy = (G[2] - G[4]) + (G[5] + G[6]) - (G[7] + G[8]);
+    if (c.force) { jx += c.shfx; jy += c.shfy; }
+    const CT RS = c.dscale + DR;                          // s * rho
+    const CT inv = Ar<true>::rcp(RS);
+    const CT ux = jx * inv, uy = jy * inv;
+    const CT u2k3 = c.k3 * fma(ux, ux, uy * uy);
+    const CT rs0 = RS * c.wt[0], rs1 = RS * c.wt[1], rs5 = RS * c.wt[5];
+    const CT wd0 = DR * c.wt[0], wd1 = DR * c.wt[1], wd5 = DR * c.wt[5];
+    CT geq[9];
+    geq[0] = fma(rs0, u2k3, wd0);
+    {
+        const CT A = fma(c.k2, ux * ux, u2k3), B = c.k1 * ux;
+        geq[1] = fma(rs1, A + B, wd1); geq[3] = fma(rs1, A - B, wd1);
+    }
+    {
+        const CT A = fma(c.k2, uy * uy, u2k3), B = c.k1 * uy;
+        geq[2] = fma(rs1, A + B, wd1); geq[4] = fma(rs1, A - B, wd1);
+    }
+    const CT d = ux + uy, e = uy - ux;
+    {
+        const CT A = fma(c.k2, d * d, u2k3), B = c.k1 * d;
+        geq[5] = fma(rs5, A + B, wd5); geq[7] = fma(rs5, A - B, wd5);
+    }
+    {
+        const CT A = fma(c.k2, e * e, u2k3), B = c.k1 * e;
+        geq[6] = fma(rs5, A + B, wd5); geq[8] = fma(rs5, A - B, wd5);
+    }
+    if (c.collision == LBM_COLLISION_TRT) {
+#pragma unroll
+        for (int i = 0; i < 9; ++i) {
+            const CT gsw = G[OPP(i)];
+            const CT eqsw = (i == 0) ? geq[0] : gsw;
+            const CT om = ((G[i] + gsw) - (geq[i] + eqsw)) * c.omega_p +
+                          ((G[i] - gsw) - (geq[i] - eqsw)) * c.omega_m;
+            out[i] = fma(om, c.trt_scale, G[i]);
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < 9; ++i) out[i] = fma(G[i] - geq[i], c.bgk_factor, G[i]);
+    }
+    if (c.force) {
+        const CT uF = c.k1 * fma(ux, c.fx, uy * c.fy);
+        CT vc[9];
+        vc[0] = CT(0); vc[1] = ux; vc[2] = uy; vc[3] = -ux; vc[4] = -uy;
+        vc[5] = d; vc[6] = e; vc[7] = -d; vc[8] = -e;
+#pragma unroll
+        for (int i = 0; i < 9; ++i)
+            out[i] = fma(c.sgw[i], fma(vc[i], c.cF4[i], c.kcF[i] - uF), out[i]);
+    }
+}
+
 // Moments of a stored cell state (Lattice::density / velocity, src/lbm.rs:
 // 117-149), with u = (j - F/2)/rho when a body force is set.
 template <bool FAST, class CT>
@@ -285,6 +345,31 @@ __device__ __forceinline__ void cell_moments(const Consts<CT>& c, const CT (&f)[
     const CT inv = A::rcp(rho);
     ux = A::mul(inv, mx);
     uy = A::mul(inv, my);
+}
+
+// Moments of a stored cell given in the step kernels' working variables.
+template <class S, bool FAST, class CT>
+__device__ __forceinline__ void domain_moments(const Consts<CT>& c, const CT (&g)[9], CT& rho,
+                                               CT& ux, CT& uy) {
+    if constexpr (Store<S>::DEV) {
+        const CT DR = ((g[0] + g[1]) + (g[2] + g[3])) + ((g[4] + g[5]) + (g[6] + g[7])) + g[8];
+        CT jx = (g[1] - g[3]) + (g[5] - g[6]) + (g[8] - g[7]);
+        CT jy = (g[2] - g[4]) + (g[5] + g[6]) - (g[7] + g[8]);
+        if (c.force) { jx -= c.shfx; jy -= c.shfy; }
+        const CT inv = Ar<true>::rcp(c.dscale + DR);
+        rho = CT(1) + DR * c.dinv;
+        ux = jx * inv;
+        uy = jy * inv;
+    } else {
+        cell_moments<FAST>(c, g, rho, ux, uy);
+    }
+}
+
+// The collision in the working variables of storage type S.
+template <class S, bool FAST, class CT>
+__device__ __forceinline__ void collide_domain(const Consts<CT>& c, const CT (&g)[9], CT (&out)[9]) {
+    if constexpr (Store<S>::DEV) collide_dev<CT>(c, g, out);
+    else collide_cell<FAST>(c, g, out);
 }
 
 // Writes the V collided cells of a thread and, when requested, their moments
@@ -314,9 +399,9 @@ __device__ __forceinline__ void store_cells(const StepArgs<typename Store<S>::CT
             if (x0 + k >= w) break;
             CT g[9];
 #pragma unroll
-            for (int i = 0; i < 9; ++i) g[i] = ST::dec(enc[i][k], a.c.wt[i], a.c.dinv);
+            for (int i = 0; i < 9; ++i) g[i] = ST::dec_dom(enc[i][k]);
             CT r, ux, uy;
-            cell_moments<FAST>(a.c, g, r, ux, uy);
+            domain_moments<S, FAST>(a.c, g, r, ux, uy);
             a.mom_rho[base + k] = float(r);
             a.mom_ux[base + k] = float(ux);
             a.mom_uy[base + k] = float(uy);
@@ -342,26 +427,26 @@ __device__ __forceinline__ void step_interior(const StepArgs<typename Store<S>::
         const S* p = base + i * PL - dr * P;
         VecIO<S, V>::load(p, raw[i]);
         edge[i] = raw[i][0];
-        if (dc == 1 && lane == 0) edge[i] = __ldg(p - 1);
-        if (dc == -1 && lane == 31) edge[i] = __ldg(p + V);
+        // edge columns wrap on the first / last tile of a periodic row
+        if (dc == 1 && lane == 0) edge[i] = __ldg(p - 1 + (x0 == 0 ? a.w : 0));
+        if (dc == -1 && lane == 31) edge[i] = __ldg(p + V - (x0 + V == a.w ? a.w : 0));
     }
     CT f[9][V];
 #pragma unroll
     for (int i = 0; i < 9; ++i) {
         const int dc = DCOL(FRAME, i);
-        const CT wi = a.c.wt[i];
         CT v[V];
-        ST::dec_vec(raw[i], v, wi, a.c.dinv);
+        ST::dec_vec_dom(raw[i], v);
         if (dc == 1) {
             const CT left = __shfl_up_sync(kFull, v[V - 1], 1);
 #pragma unroll
             for (int k = V - 1; k > 0; --k) v[k] = v[k - 1];
-            v[0] = lane == 0 ? ST::dec(edge[i], wi, a.c.dinv) : left;
+            v[0] = lane == 0 ? ST::dec_dom(edge[i]) : left;
         } else if (dc == -1) {
             const CT right = __shfl_down_sync(kFull, v[0], 1);
 #pragma unroll
             for (int k = 0; k < V - 1; ++k) v[k] = v[k + 1];
-            v[V - 1] = lane == 31 ? ST::dec(edge[i], wi, a.c.dinv) : right;
+            v[V - 1] = lane == 31 ? ST::dec_dom(edge[i]) : right;
         }
 #pragma unroll
         for (int k = 0; k < V; ++k) f[i][k] = v[k];
@@ -371,13 +456,13 @@ __device__ __forceinline__ void step_interior(const StepArgs<typename Store<S>::
         CT g[9], o[9];
 #pragma unroll
         for (int i = 0; i < 9; ++i) g[i] = f[i][k];
-        collide_cell<FAST>(a.c, g, o);
+        collide_domain<S, FAST>(a.c, g, o);
 #pragma unroll
         for (int i = 0; i < 9; ++i) f[i][k] = o[i];
     }
     S enc[9][V];
 #pragma unroll
-    for (int i = 0; i < 9; ++i) ST::enc_vec(f[i], enc[i], a.c.wt[i], a.c.dscale);
+    for (int i = 0; i < 9; ++i) ST::enc_vec_dom(f[i], enc[i]);
     store_cells<S, V, FAST>(a, y, x0, enc);
 }
 
@@ -478,8 +563,8 @@ __device__ __forceinline__ void step_general(const StepArgs<typename Store<S>::C
         const int dc = DCOL(FRAME, i), dr = DROW(FRAME, i);
         const CT wi = a.c.wt[i];
         CT v[V];
-        ST::dec_vec(raw[i], v, wi, a.c.dinv);
-        const CT e = ST::dec(edge[i], wi, a.c.dinv);
+        ST::dec_vec_dom(raw[i], v);
+        const CT e = ST::dec_dom(edge[i]);
         uint32_t xz = 0u, xb = 0u;
         if (dc == 1) {
             const CT left = __shfl_up_sync(kFull, v[V - 1], 1);
@@ -501,7 +586,7 @@ __device__ __forceinline__ void step_general(const StepArgs<typename Store<S>::C
                     if (sx >= w) {
                         if (xper) {
                             if (!(k == V - 1 && sx == w))   // not already the edge load
-                                v[k] = ST::dec(__ldg(prow + (sx % w)), wi, a.c.dinv);
+                                v[k] = ST::dec_dom(__ldg(prow + (sx % w)));
                         } else if (xm == 2) {
                             xb |= 1u << k;
                         } else {
@@ -517,8 +602,9 @@ __device__ __forceinline__ void step_general(const StepArgs<typename Store<S>::C
         const uint32_t z = (cls == 1 ? FULL : xz) & ~b;
         if (has_solid && halfway) b |= (mrow[1 - dr] >> (1 - dc)) & FULL;
         if (z) {
+            const CT zv = ST::zero_dom(wi, a.c.dscale);
 #pragma unroll
-            for (int k = 0; k < V; ++k) if ((z >> k) & 1u) v[k] = CT(0);
+            for (int k = 0; k < V; ++k) if ((z >> k) & 1u) v[k] = zv;
         }
 #pragma unroll
         for (int k = 0; k < V; ++k) f[i][k] = v[k];
@@ -533,7 +619,7 @@ __device__ __forceinline__ void step_general(const StepArgs<typename Store<S>::C
             IO::load(src + OPP(i) * PL + int64_t(y) * P + xl, own);
 #pragma unroll
             for (int k = 0; k < V; ++k)
-                if ((bnc[i] >> k) & 1u) f[i][k] = ST::dec(own[k], a.c.wt[OPP(i)], a.c.dinv);
+                if ((bnc[i] >> k) & 1u) f[i][k] = ST::dec_dom(own[k]);
         }
     }
 
@@ -559,12 +645,12 @@ __device__ __forceinline__ void step_general(const StepArgs<typename Store<S>::C
         CT g[9], o[9];
 #pragma unroll
         for (int i = 0; i < 9; ++i) g[i] = f[i][k];
-        collide_cell<FAST>(a.c, g, o);
+        collide_domain<S, FAST>(a.c, g, o);
 #pragma unroll
         for (int i = 0; i < 9; ++i) f[i][k] = o[i];
     }
 #pragma unroll
-    for (int i = 0; i < 9; ++i) ST::enc_vec(f[i], enc[i], a.c.wt[i], a.c.dscale);
+    for (int i = 0; i < 9; ++i) ST::enc_vec_dom(f[i], enc[i]);
 
     if (own_solid && halfway) {
         // Half-way mode: solid nodes keep their populations.
@@ -582,52 +668,46 @@ __device__ __forceinline__ void step_general(const StepArgs<typename Store<S>::C
     store_cells<S, V, FAST>(a, y, x0, enc);
 }
 
-// Interior tiles of the whole lattice: grid (tiles per row, rows / warps per
-// block); a warp whose tile is flagged leaves at once (the general kernel
-// owns it).
+// One step over the whole lattice in one launch.  With tile flags: the first
+// ceil(ngtiles / rows) blocks take the flagged tiles from the list a.gtiles
+// (entry = row * ntiles + tile), one warp per entry, so their longer latency
+// overlaps the rest; the remaining blocks cover every (row, tile) in row-major
+// order and run the interior path, leaving tiles flagged 1 to the list.
+// Without tile flags, every tile takes the general path.
 template <class S, int V, int FRAME, bool FAST>
 __global__ void __launch_bounds__(256, (sizeof(typename Store<S>::CT) == 4 && V <= 4) ? 3 : 1)
-lbm_interior_kernel(const StepArgs<typename Store<S>::CT> a) {
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
-    if (y >= a.h) return;
-    if (a.tflags[int64_t(y) * a.ntiles + blockIdx.x] != 0) return;     // warp-uniform
-    step_interior<S, V, FRAME, FAST>(a, y, (blockIdx.x * 32 + threadIdx.x) * V, threadIdx.x);
-}
-
-// The flagged tiles (a lattice edge or a solid within one cell), one warp per
-// entry of the list a.gtiles (entry = row * ntiles + tile); with no list,
-// every tile of the lattice (grid as the interior kernel's).
-template <class S, int V, int FRAME, bool FAST>
-__global__ void __launch_bounds__(256)
 lbm_step_kernel(const StepArgs<typename Store<S>::CT> a) {
-    int y, tile;
-    if (a.gtiles != nullptr) {
-        const int e = blockIdx.x * blockDim.y + threadIdx.y;
+    const int rows = blockDim.y;
+    const int gblocks = a.tflags != nullptr ? (a.ngtiles + rows - 1) / rows : 0;
+    const int b = blockIdx.x;
+    if (b < gblocks) {
+        const int e = b * rows + threadIdx.y;
         if (e >= a.ngtiles) return;
         const uint32_t t = a.gtiles[e];
-        y = int(t / uint32_t(a.ntiles));
-        tile = int(t - uint32_t(y) * uint32_t(a.ntiles));
-    } else {
-        y = blockIdx.y * blockDim.y + threadIdx.y;
-        if (y >= a.h) return;
-        tile = blockIdx.x;
+        const int y = int(t / uint32_t(a.ntiles));
+        step_general<S, V, FRAME, FAST>(a, y, int(t - uint32_t(y) * uint32_t(a.ntiles)), threadIdx.x);
+        return;
     }
-    step_general<S, V, FRAME, FAST>(a, y, tile, threadIdx.x);
+    const int ib = b - gblocks;
+    const int by = ib / a.ntiles, tile = ib - by * a.ntiles;
+    const int y = by * rows + threadIdx.y;
+    if (y >= a.h) return;                                                  // warp-uniform
+    if (a.tflags == nullptr) {
+        step_general<S, V, FRAME, FAST>(a, y, tile, threadIdx.x);
+        return;
+    }
+    if (a.tflags[int64_t(y) * a.ntiles + tile] == 1) return;             // owned by the list
+    step_interior<S, V, FRAME, FAST>(a, y, (tile * 32 + threadIdx.x) * V, threadIdx.x);
 }
 
 template <class S, int V, int FRAME, bool FAST>
 void launch_step_tv(const StepArgs<typename Store<S>::CT>& a, int rows, cudaStream_t stream) {
-    const dim3 block(32, rows);
-    const dim3 full((a.w + 32 * V - 1) / (32 * V), (a.h + rows - 1) / rows);
-    if (a.tflags != nullptr) {
-        lbm_interior_kernel<S, V, FRAME, FAST><<<full, block, 0, stream>>>(a);
-        if (a.ngtiles > 0)
-            lbm_step_kernel<S, V, FRAME, FAST><<<(a.ngtiles + rows - 1) / rows, block, 0, stream>>>(a);
-    } else {
-        StepArgs<typename Store<S>::CT> b = a;
-        b.gtiles = nullptr;
-        lbm_step_kernel<S, V, FRAME, FAST><<<full, block, 0, stream>>>(b);
-    }
+    const int ntiles = (a.w + 32 * V - 1) / (32 * V);
+    const int rowblocks = (a.h + rows - 1) / rows;
+    const int gblocks = a.tflags != nullptr ? (a.ngtiles + rows - 1) / rows : 0;
+    StepArgs<typename Store<S>::CT> b = a;
+    b.ntiles = ntiles;
+    lbm_step_kernel<S, V, FRAME, FAST><<<gblocks + ntiles * rowblocks, dim3(32, rows), 0, stream>>>(b);
 }
 
 // One step: the interior kernel plus the general kernel over the flagged
