@@ -54,6 +54,14 @@ class LBMHealth(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
 
 
+class LBMDesc(ctypes.Structure):
+    _fields_ = [
+        ("w", ctypes.c_int), ("h", ctypes.c_int), ("tau", ctypes.c_float),
+        ("flags", ctypes.c_int), ("fx", ctypes.c_float), ("fy", ctypes.c_float),
+        ("solid", ctypes.c_void_p),
+    ]
+
+
 class LBMError(RuntimeError):
     """A negative status of the C ABI (the reference panics in these cases)."""
 
@@ -97,6 +105,14 @@ SIGNATURES = {
     "lbm_set_tile": (_i32, [_vp, _i32, _i32]),
     "lbm_check_device_noalloc": (_i32, [_vp, _i32, _i32, _i32, _i32, _i64, _f32, _f32, _vp,
                                         ctypes.POINTER(LBMHealth)]),
+    "lbm_batch_create": (_i32, [_i32, ctypes.POINTER(LBMDesc), _i32, ctypes.POINTER(_vp)]),
+    "lbm_batch_destroy": (_i32, [_vp]),
+    "lbm_batch_size": (_i32, [_vp, ctypes.POINTER(_i32)]),
+    "lbm_batch_lattice": (_i32, [_vp, _i32, ctypes.POINTER(_vp)]),
+    "lbm_batch_step": (_i32, [_vp, _i32]),
+    "lbm_batch_synchronize": (_i32, [_vp]),
+    "lbm_batch_set_stream": (_i32, [_vp, _vp]),
+    "lbm_batch_autotune": (_i32, [_vp, ctypes.c_char_p, _i32]),
 }
 
 _lock = threading.Lock()

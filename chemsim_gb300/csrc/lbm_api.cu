@@ -70,7 +70,7 @@ int default_cells(int precision) {
 
 bool valid_cells(int precision, int v) {
     switch (precision) {
-        case LBM_F32: return v == 4 || v == 8;
+        case LBM_F32: return v == 2 || v == 4 || v == 8;
         case LBM_F64: return v == 2;
         default: return v == 4 || v == 8;
     }
@@ -84,35 +84,7 @@ int grid_for(int64_t n, int block) {
 
 }  // namespace
 
-struct lbm_lattice {
-    int w = 0, h = 0, precision = 0, flags = 0;
-    int pitch = 0, mpitch = 0;
-    int64_t plane = 0;
-    size_t esize = 0;
-    void* buf[2] = {nullptr, nullptr};
-    int cur = 0;
-    uint8_t* solid = nullptr;
-    bool has_solid = false;
-    float* mom[3] = {nullptr, nullptr, nullptr};
-    bool mom_valid = false;
-    void* staging = nullptr;
-    size_t staging_bytes = 0;
-    HealthPartial* health = nullptr;      // kHealthBlocks partials + 1 result
-    uint8_t* tflags = nullptr;            // h x ceil(w / 32) bytes
-    int ntiles = 0;
-    uint32_t* gtiles = nullptr;           // list of flagged tiles
-    int ngtiles = 0;
-    size_t gtiles_cap = 0;
-    int collision = LBM_COLLISION_BGK;
-    float tau = 1.f, tau_minus = 1.f, dx = 1.f, dt = 1.f, fx = 0.f, fy = 0.f;
-    float time = 0.f;
-    int64_t steps = 0;
-    cudaStream_t own = nullptr, stream = nullptr;
-    cudaGraphExec_t graph[2] = {nullptr, nullptr};
-    bool dirty = true;
-    int vcells = 0, rows = 4;
-    int dev = 0;
-};
+#include "lbm_handle.cuh"
 
 namespace {
 
@@ -161,21 +133,8 @@ Consts<CT> make_consts(const lbm_lattice* L) {
 
 template <class S>
 cudaError_t launch_one_t(lbm_lattice* L, int from, bool moments) {
-    using CT = typename Store<S>::CT;
-    StepArgs<CT> a{};
-    a.src = L->buf[from];
-    a.dst = L->buf[from ^ 1];
-    a.solid = L->has_solid ? L->solid : nullptr;
-    a.tflags = L->tflags;
-    a.ntiles = L->ntiles;
-    a.gtiles = L->gtiles;
-    a.ngtiles = L->ngtiles;
-    if (moments) { a.mom_rho = L->mom[0]; a.mom_ux = L->mom[1]; a.mom_uy = L->mom[2]; }
-    a.w = L->w; a.h = L->h; a.pitch = L->pitch; a.mpitch = L->mpitch; a.plane = L->plane;
-    a.flags = L->flags;
-    a.c = make_consts<CT>(L);
-    return launch_step<S>(a, (L->flags & LBM_FRAME_XY) ? 1 : 0, (L->flags & LBM_FAST) != 0,
-                          L->vcells, L->rows, L->stream);
+    return launch_step<S>(lattice_args<S>(L, from, moments), (L->flags & LBM_FRAME_XY) ? 1 : 0,
+                          (L->flags & LBM_FAST) != 0, L->vcells, L->rows, L->stream);
 }
 
 cudaError_t launch_one(lbm_lattice* L, int from, bool moments) {
@@ -230,12 +189,13 @@ int refresh_tiles(lbm_lattice* L) {
     const int tile_w = 32 * L->vcells;
     L->ntiles = (L->w + tile_w - 1) / tile_w;
     const int64_t n = int64_t(L->h) * L->ntiles;
-    // Edge tiles of a periodic-x row whose width is a whole number of tiles
-    // only need wrapped edge addresses: the interior kernel takes them.
-    const int xwrap = ((L->flags & 3) == LBM_X_PERIODIC && L->w % tile_w == 0) ? 1 : 0;
+    // Edge tiles of periodic axes only need wrapped addresses: the interior
+    // path takes them.
+    const int xper = (L->flags & 3) == LBM_X_PERIODIC ? 1 : 0;
+    const int yper = ((L->flags >> 2) & 3) == 1 ? 1 : 0;
     tile_flags_kernel<<<grid_for(n, 256), 256, 0, L->stream>>>(
         L->tflags, L->has_solid ? L->solid : nullptr, L->w, L->h, L->mpitch, tile_w, L->ntiles,
-        xwrap);
+        xper, yper);
     LBM_CUDA(cudaGetLastError());
     // Compact the flagged tiles on the host (row-major order, deterministic).
     std::vector<uint8_t> flags(static_cast<size_t>(n));
@@ -258,6 +218,7 @@ int refresh_tiles(lbm_lattice* L) {
     LBM_CUDA(cudaStreamSynchronize(L->stream));
     L->ngtiles = int(list.size());
     L->dirty = true;
+    ++L->version;
     return LBM_OK;
 }
 
@@ -400,6 +361,37 @@ int steps_impl(lbm_lattice* L, int nsteps, bool moments) {
 namespace lbmk {
 void set_last_error(const std::string& msg) { g_err = msg; }
 
+int lattice_fail(int code, const std::string& msg) { return fail(code, msg); }
+
+template <class S>
+StepArgs<typename Store<S>::CT> lattice_args(const lbm_lattice* L, int from, bool moments) {
+    using CT = typename Store<S>::CT;
+    StepArgs<CT> a{};
+    a.src = L->buf[from];
+    a.dst = L->buf[from ^ 1];
+    a.solid = L->has_solid ? L->solid : nullptr;
+    a.tflags = L->tflags;
+    a.ntiles = L->ntiles;
+    a.gtiles = L->gtiles;
+    a.ngtiles = L->ngtiles;
+    if (moments) { a.mom_rho = L->mom[0]; a.mom_ux = L->mom[1]; a.mom_uy = L->mom[2]; }
+    a.w = L->w; a.h = L->h; a.pitch = L->pitch; a.mpitch = L->mpitch; a.plane = L->plane;
+    a.flags = L->flags;
+    a.c = make_consts<CT>(L);
+    return a;
+}
+template StepArgs<float> lattice_args<float>(const lbm_lattice*, int, bool);
+template StepArgs<double> lattice_args<double>(const lbm_lattice*, int, bool);
+template StepArgs<float> lattice_args<__half>(const lbm_lattice*, int, bool);
+template StepArgs<float> lattice_args<__nv_bfloat16>(const lbm_lattice*, int, bool);
+
+void lattice_advance(lbm_lattice* L, int nsteps) {
+    if (nsteps & 1) L->cur ^= 1;
+    for (int k = 0; k < nsteps; ++k) L->time += L->dt;
+    L->steps += nsteps;
+    L->mom_valid = false;
+}
+
 __global__ void normalize_mask_kernel(uint8_t* __restrict__ m, int w, int h, int mpitch) {
     const int64_t n = int64_t(w) * h;
     for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < n;
@@ -411,24 +403,28 @@ __global__ void normalize_mask_kernel(uint8_t* __restrict__ m, int w, int h, int
 }
 
 __global__ void tile_flags_kernel(uint8_t* __restrict__ tflags, const uint8_t* __restrict__ solid,
-                                  int w, int h, int mpitch, int tile_w, int ntiles, int xwrap) {
+                                  int w, int h, int mpitch, int tile_w, int ntiles, int xper,
+                                  int yper) {
     const int64_t n = int64_t(h) * ntiles;
     for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < n;
          t += int64_t(gridDim.x) * blockDim.x) {
         const int y = int(t / ntiles), tt = int(t - int64_t(y) * ntiles);
         const int xs = tt * tile_w;
         const bool xedge = xs == 0 || xs + tile_w >= w;
-        bool gen = y == 0 || y == h - 1 || (xedge && !xwrap);
+        const bool yedge = y == 0 || y == h - 1;
+        bool gen = (xedge && !xper) || (yedge && !yper);
         if (!gen && solid != nullptr) {
+            const int xe = min(xs + tile_w, w);          // columns xs-1 .. xe, wrapped
             for (int r = y - 1; r <= y + 1 && !gen; ++r) {
-                const uint8_t* row = solid + int64_t(r) * mpitch;
-                for (int c = xs - 1; c <= xs + tile_w; ++c) {
+                const int rr = r < 0 ? r + h : (r >= h ? r - h : r);
+                const uint8_t* row = solid + int64_t(rr) * mpitch;
+                for (int c = xs - 1; c <= xe; ++c) {
                     const int cc = c < 0 ? c + w : (c >= w ? c - w : c);
                     if (row[cc]) { gen = true; break; }
                 }
             }
         }
-        tflags[t] = gen ? 1 : (xedge ? 2 : 0);
+        tflags[t] = gen ? 1 : ((xedge || yedge) ? 2 : 0);
     }
 }
 
@@ -528,7 +524,7 @@ int lbm_set_discretization(lbm_lattice* L, float dx, float dt) {
     if (int rc = check_handle(L)) return rc;
     if (!(dx > 0.f) || !(dt > 0.f) || !std::isfinite(dx) || !std::isfinite(dt))
         return fail(LBM_ERR_INVALID_ARGUMENT, "delta_x and delta_t must be finite and > 0");
-    L->dx = dx; L->dt = dt; L->dirty = true; L->mom_valid = false;
+    L->dx = dx; L->dt = dt; L->dirty = true; ++L->version; L->mom_valid = false;
     return LBM_OK;
 }
 
@@ -543,6 +539,7 @@ int lbm_set_collision(lbm_lattice* L, int kind, float tau, float tau_minus) {
     L->collision = kind; L->tau = tau;
     L->tau_minus = kind == LBM_COLLISION_TRT ? tau_minus : 1.f;
     L->dirty = true;
+    ++L->version;
     return LBM_OK;
 }
 
@@ -640,7 +637,7 @@ int lbm_set_force(lbm_lattice* L, float fx, float fy) {
     if (int rc = check_handle(L)) return rc;
     if (!std::isfinite(fx) || !std::isfinite(fy))
         return fail(LBM_ERR_INVALID_ARGUMENT, "force must be finite");
-    L->fx = fx; L->fy = fy; L->dirty = true; L->mom_valid = false;
+    L->fx = fx; L->fy = fy; L->dirty = true; ++L->version; L->mom_valid = false;
     return LBM_OK;
 }
 
@@ -734,7 +731,7 @@ int lbm_set_tile(lbm_lattice* L, int cells_per_thread, int rows_per_block) {
     if (r < 1 || r > 8 || (L->h + r - 1) / r > 65535 || 32 * r > 256)
         return fail(LBM_ERR_INVALID_ARGUMENT, "rows_per_block must be in [1, 8] and cover h");
     DeviceGuard g(L->dev);
-    L->vcells = v; L->rows = r; L->dirty = true;
+    L->vcells = v; L->rows = r; L->dirty = true; ++L->version;
     if (int rc = refresh_tiles(L)) return rc;
     LBM_CUDA(cudaStreamSynchronize(L->stream));
     return LBM_OK;

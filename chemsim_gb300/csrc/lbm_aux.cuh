@@ -121,12 +121,13 @@ __global__ void moments_kernel(const S* __restrict__ f, float* __restrict__ rho,
 // multiply that needs 0/1 bytes).
 __global__ void normalize_mask_kernel(uint8_t* __restrict__ m, int w, int h, int mpitch);
 
-// Per (row, warp tile of tile_w cells): 1 when the tile touches a lattice
-// edge row, a non-wrapping edge column or has a solid cell within one cell of
-// it; 2 for an edge tile of a wrapping (periodic, whole tiles) row; 0
-// otherwise.  Tiles flagged 0 or 2 take the interior kernel.
+// Per (row, warp tile of tile_w cells): 1 when the tile reaches a lattice
+// edge that is not periodic, or has a solid cell within one cell of it (the
+// general path); 2 when it reaches only periodic edges (the wrapping
+// interior path); 0 otherwise (the lean interior path).
 __global__ void tile_flags_kernel(uint8_t* __restrict__ tflags, const uint8_t* __restrict__ solid,
-                                  int w, int h, int mpitch, int tile_w, int ntiles, int xwrap);
+                                  int w, int h, int mpitch, int tile_w, int ntiles, int xper,
+                                  int yper);
 
 // Sets the message lbm_last_error_string returns on this thread.
 void set_last_error(const std::string& msg);

@@ -1,0 +1,53 @@
+// lbm_handle.cuh — the lattice handle shared by the single-lattice and the
+// batched entry points (host-side, internal to liblbm_cuda.so).
+#pragma once
+
+#include <string>
+
+#include "lbm_aux.cuh"
+
+struct lbm_lattice {
+    int w = 0, h = 0, precision = 0, flags = 0;
+    int pitch = 0, mpitch = 0;
+    int64_t plane = 0;
+    size_t esize = 0;
+    void* buf[2] = {nullptr, nullptr};
+    int cur = 0;
+    uint8_t* solid = nullptr;
+    bool has_solid = false;
+    float* mom[3] = {nullptr, nullptr, nullptr};
+    bool mom_valid = false;
+    void* staging = nullptr;
+    size_t staging_bytes = 0;
+    lbmk::HealthPartial* health = nullptr;  // kHealthBlocks partials + 1 result
+    uint8_t* tflags = nullptr;            // h x ceil(w / 32) bytes
+    int ntiles = 0;
+    uint32_t* gtiles = nullptr;           // list of flagged tiles
+    int ngtiles = 0;
+    size_t gtiles_cap = 0;
+    int collision = LBM_COLLISION_BGK;
+    float tau = 1.f, tau_minus = 1.f, dx = 1.f, dt = 1.f, fx = 0.f, fy = 0.f;
+    float time = 0.f;
+    int64_t steps = 0;
+    cudaStream_t own = nullptr, stream = nullptr;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    bool dirty = true;                    // captured graphs are stale
+    uint64_t version = 0;                 // bumped on every change of the step arguments
+    int vcells = 0, rows = 4;
+    int dev = 0;
+};
+
+namespace lbmk {
+
+// Step arguments of lattice L from buffer `from` (moments written when asked).
+template <class S>
+StepArgs<typename Store<S>::CT> lattice_args(const lbm_lattice* L, int from, bool moments);
+
+// Bookkeeping after nsteps steps run by someone else (the batch kernel):
+// buffer parity, State::time, the step count and the moment cache.
+void lattice_advance(lbm_lattice* L, int nsteps);
+
+// Records msg for lbm_last_error_string and returns code.
+int lattice_fail(int code, const std::string& msg);
+
+}  // namespace lbmk

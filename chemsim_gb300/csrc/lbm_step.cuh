@@ -409,9 +409,9 @@ __device__ __forceinline__ void store_cells(const StepArgs<typename Store<S>::CT
     }
 }
 
-// Interior warp tile: every source cell is inside the lattice and fluid (the
-// tile flags say so), so a step is 9 vector loads, 6 shuffles and two edge
-// scalars per lane, the collision and 9 vector stores.
+// Interior warp tile (flag 0): every source cell is inside the lattice and
+// fluid, so a step is 9 vector loads, 6 shuffles and two edge scalars per
+// lane, the collision and 9 vector stores.
 template <class S, int V, int FRAME, bool FAST>
 __device__ __forceinline__ void step_interior(const StepArgs<typename Store<S>::CT>& a, int y,
                                               int x0, int lane) {
@@ -427,9 +427,8 @@ __device__ __forceinline__ void step_interior(const StepArgs<typename Store<S>::
         const S* p = base + i * PL - dr * P;
         VecIO<S, V>::load(p, raw[i]);
         edge[i] = raw[i][0];
-        // edge columns wrap on the first / last tile of a periodic row
-        if (dc == 1 && lane == 0) edge[i] = __ldg(p - 1 + (x0 == 0 ? a.w : 0));
-        if (dc == -1 && lane == 31) edge[i] = __ldg(p + V - (x0 + V == a.w ? a.w : 0));
+        if (dc == 1 && lane == 0) edge[i] = __ldg(p - 1);
+        if (dc == -1 && lane == 31) edge[i] = __ldg(p + V);
     }
     CT f[9][V];
 #pragma unroll
@@ -464,6 +463,86 @@ __device__ __forceinline__ void step_interior(const StepArgs<typename Store<S>::
 #pragma unroll
     for (int i = 0; i < 9; ++i) ST::enc_vec_dom(f[i], enc[i]);
     store_cells<S, V, FAST>(a, y, x0, enc);
+}
+
+// One time step of one lattice.  Phase A issues every global load of the
+// thread (3 mask rows, 9 population vectors and the warp-edge scalars) before
+// any of them is consumed, so a thread has ~150 B in flight and pays one
+// memory latency; phase B realigns the +-1 column shifts with shuffles and
+// classifies boundary links; phase C fetches the cell's own opposite
+// populations for bounce-back links (only near walls and solids); phase D
+// collides and stores.
+// Periodic-edge warp tile (flag 2): every source cell is fluid and the tile
+// reaches only periodic lattice edges.  A step is 9 vector loads, 6 shuffles, two edge
+// scalars per lane, the collision and 9 vector stores; the edge rows and
+// columns wrap.  On a partial last tile, lanes past the edge only feed the
+// shuffles, and the lane holding column w - 1 takes column 0 for the cell
+// whose source lies past the edge.
+template <class S, int V, int FRAME, bool FAST>
+__device__ __forceinline__ void step_interior_wrap(const StepArgs<typename Store<S>::CT>& a, int y,
+                                              int x0, int lane) {
+    using CT = typename Store<S>::CT;
+    using ST = Store<S>;
+    const int w = a.w, h = a.h;
+    const int64_t P = a.pitch, PL = a.plane;
+    const S* __restrict__ src = static_cast<const S*>(a.src);
+    const int ym1 = y == 0 ? h - 1 : y - 1, yp1 = y == h - 1 ? 0 : y + 1;
+    const int xl = x0 < w ? x0 : 0;                 // idle lanes read a valid chunk
+    const bool last = x0 < w && x0 + V >= w;        // this chunk holds column w - 1
+    S raw[9][V];
+    S edge[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+        const int dc = DCOL(FRAME, i), dr = DROW(FRAME, i);
+        const int sr = dr == 1 ? ym1 : (dr == -1 ? yp1 : y);
+        const S* prow = src + i * PL + int64_t(sr) * P;
+        VecIO<S, V>::load(prow + xl, raw[i]);
+        edge[i] = raw[i][0];
+        if (dc == 1 && lane == 0) edge[i] = __ldg(prow + (x0 == 0 ? w - 1 : x0 - 1));
+        if (dc == -1) {
+            if (last) edge[i] = __ldg(prow);               // column w wraps to 0
+            else if (lane == 31) edge[i] = __ldg(prow + x0 + V);
+        }
+    }
+    CT f[9][V];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+        const int dc = DCOL(FRAME, i);
+        CT v[V];
+        ST::dec_vec_dom(raw[i], v);
+        if (dc == 1) {
+            const CT left = __shfl_up_sync(kFull, v[V - 1], 1);
+#pragma unroll
+            for (int k = V - 1; k > 0; --k) v[k] = v[k - 1];
+            v[0] = lane == 0 ? ST::dec_dom(edge[i]) : left;
+        } else if (dc == -1) {
+            const CT right = __shfl_down_sync(kFull, v[0], 1);
+#pragma unroll
+            for (int k = 0; k < V - 1; ++k) v[k] = v[k + 1];
+            const CT e = ST::dec_dom(edge[i]);
+            v[V - 1] = lane == 31 ? e : right;
+            if (last) {
+#pragma unroll
+                for (int k = 0; k < V; ++k)
+                    if (x0 + k == w - 1) v[k] = e;
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < V; ++k) f[i][k] = v[k];
+    }
+#pragma unroll
+    for (int k = 0; k < V; ++k) {
+        CT g[9], o[9];
+#pragma unroll
+        for (int i = 0; i < 9; ++i) g[i] = f[i][k];
+        collide_domain<S, FAST>(a.c, g, o);
+#pragma unroll
+        for (int i = 0; i < 9; ++i) f[i][k] = o[i];
+    }
+    S enc[9][V];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) ST::enc_vec_dom(f[i], enc[i]);
+    if (x0 < w) store_cells<S, V, FAST>(a, y, x0, enc);
 }
 
 // One time step of one lattice.  Phase A issues every global load of the
@@ -696,8 +775,10 @@ lbm_step_kernel(const StepArgs<typename Store<S>::CT> a) {
         step_general<S, V, FRAME, FAST>(a, y, tile, threadIdx.x);
         return;
     }
-    if (a.tflags[int64_t(y) * a.ntiles + tile] == 1) return;             // owned by the list
-    step_interior<S, V, FRAME, FAST>(a, y, (tile * 32 + threadIdx.x) * V, threadIdx.x);
+    const uint8_t flag = a.tflags[int64_t(y) * a.ntiles + tile];        // warp-uniform
+    if (flag == 1) return;                                                 // owned by the list
+    if (flag == 0) step_interior<S, V, FRAME, FAST>(a, y, (tile * 32 + threadIdx.x) * V, threadIdx.x);
+    else step_interior_wrap<S, V, FRAME, FAST>(a, y, (tile * 32 + threadIdx.x) * V, threadIdx.x);
 }
 
 template <class S, int V, int FRAME, bool FAST>

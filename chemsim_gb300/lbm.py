@@ -169,6 +169,89 @@ class Lattice:
         return base.value, plane.value, pitch.value
 
 
+class _Member(Lattice):
+    """A lattice owned by a Batch (not destroyed on its own)."""
+
+    def __init__(self, lib, handle, w, h, flags):
+        self._lib = lib
+        self._h = handle
+        self.w, self.h, self.precision, self.flags = w, h, F32, flags
+
+    def close(self):
+        self._h = ctypes.c_void_p()
+
+
+class Batch:
+    """Many independent f32 lattices stepped together (lbm_batch_*).
+
+    specs: objects with w, h, tau, flags, force and solid (see
+    chemsim_gb300.workloads.LatticeSpec).  `flags` of the batch carries
+    FRAME_XY / FAST for every member.
+    """
+
+    def __init__(self, specs, flags: int = FRAME_XY | FAST):
+        self._lib = _lib.load()
+        descs = (_lib.LBMDesc * len(specs))()
+        self._masks = []
+        for d, sp in zip(descs, specs):
+            d.w, d.h, d.tau = int(sp.w), int(sp.h), float(sp.tau)
+            d.flags = int(sp.flags) & ~(FRAME_XY | FAST)
+            d.fx, d.fy = float(sp.force[0]), float(sp.force[1])
+            if sp.solid is not None and np.any(sp.solid):
+                m = np.ascontiguousarray(sp.solid, dtype=np.uint8)
+                self._masks.append(m)
+                d.solid = m.ctypes.data
+            else:
+                d.solid = None
+        self._b = ctypes.c_void_p()
+        check(self._lib.lbm_batch_create(len(specs), descs, int(flags), ctypes.byref(self._b)))
+        self._masks = []
+        self.members = []
+        for i, sp in enumerate(specs):
+            hnd = ctypes.c_void_p()
+            check(self._lib.lbm_batch_lattice(self._b, i, ctypes.byref(hnd)))
+            self.members.append(_Member(self._lib, hnd, int(sp.w), int(sp.h),
+                                        (int(sp.flags) & ~(FRAME_XY | FAST)) | flags))
+
+    def __len__(self):
+        return len(self.members)
+
+    def __getitem__(self, i) -> Lattice:
+        return self.members[i]
+
+    def step(self, nsteps: int = 1):
+        check(self._lib.lbm_batch_step(self._b, int(nsteps)))
+
+    def synchronize(self):
+        check(self._lib.lbm_batch_synchronize(self._b))
+
+    def set_stream(self, stream_ptr):
+        check(self._lib.lbm_batch_set_stream(self._b, ctypes.c_void_p(stream_ptr or 0)))
+
+    def autotune(self, cache_path: str | None = None, steps_per_trial: int = 0):
+        path = cache_path.encode() if cache_path else None
+        check(self._lib.lbm_batch_autotune(self._b, path, int(steps_per_trial)))
+
+    def close(self):
+        if self._b:
+            for m in self.members:
+                m.close()
+            self._lib.lbm_batch_destroy(self._b)
+            self._b = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
 # ---------------------------------------------------------------------------
 # lbm.rs surface
 # ---------------------------------------------------------------------------

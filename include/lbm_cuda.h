@@ -191,10 +191,52 @@ int lbm_check_device_noalloc(const void* populations, int precision, int w, int 
                              int row_pitch, int64_t plane_stride, float delta_x,
                              float delta_t, void* stream, lbm_health* out);
 
-/* Tile of the fused step: cells per thread along x (f32: 4 or 8; f64: 2;
+/* Tile of the fused step: cells per thread along x (f32: 2, 4 or 8; f64: 2;
  * 16-bit: 4 or 8) and warps (rows) per block (1..8); 0 keeps the default.
  * No reference counterpart (tuning knob of the GB300 kernel).            */
 int lbm_set_tile(lbm_lattice* lat, int cells_per_thread, int rows_per_block);
+
+/* ---- batches of independent lattices ----------------------------------- */
+/* No reference counterpart: many lattices of uneven sizes and relaxation
+ * times advanced together by one persistent launch per time step.          */
+
+typedef struct lbm_batch lbm_batch;
+
+/* One member of a batch: size, tau, boundary flags (axes and solid mode;
+ * the frame and LBM_FAST are the batch's), body force and an optional host
+ * solid mask (w*h bytes, row-major y*w+x, nonzero = solid).              */
+typedef struct lbm_desc {
+    int w, h;
+    float tau;
+    int flags;
+    float fx, fy;
+    const uint8_t* solid;
+} lbm_desc;
+
+/* Creates n f32 member lattices (at rest equilibrium) that step together.
+ * flags: LBM_FRAME_XY and/or LBM_FAST for every member.  Members run on the
+ * batch's CUDA stream; reach them with lbm_batch_lattice and use any
+ * single-lattice entry point on them (initialise, geometry, moments, check)
+ * except lbm_set_stream.  Destroying the batch destroys its members.     */
+int lbm_batch_create(int n, const lbm_desc* descs, int flags, lbm_batch** out);
+int lbm_batch_destroy(lbm_batch* batch);
+int lbm_batch_size(lbm_batch* batch, int* n);
+int lbm_batch_lattice(lbm_batch* batch, int index, lbm_lattice** out);
+
+/* Advances every member nsteps steps (one persistent launch per step,
+ * replayed from a CUDA graph); each member's time and step count advance as
+ * with lbm_step.  Asynchronous on the batch's stream.                      */
+int lbm_batch_step(lbm_batch* batch, int nsteps);
+int lbm_batch_synchronize(lbm_batch* batch);
+int lbm_batch_set_stream(lbm_batch* batch, void* stream);
+
+/* Picks the warp-tile width (cells per thread) for each width class of the
+ * members (<= 96, <= 192, <= 384, <= 768, wider) by timing the candidates on
+ * the class's own members, whose state (populations, time, step count) is
+ * saved before and restored after; applies it and caches the choice in the
+ * JSON file cache_path (NULL: no cache).  A cached entry for this GPU and
+ * mode is reused without timing.  steps_per_trial <= 0 selects 24.         */
+int lbm_batch_autotune(lbm_batch* batch, const char* cache_path, int steps_per_trial);
 
 #ifdef __cplusplus
 }

@@ -127,6 +127,22 @@ def test_strict_f32_bit_exact(gpu, flags, size):
     assert np.array_equal(rho, r2) and np.array_equal(ux, x2) and np.array_equal(uy, y2)
 
 
+@pytest.mark.parametrize("flags", [X_PERIODIC | Y_PERIODIC, X_PERIODIC | Y_PERIODIC | FRAME_XY,
+                                   X_PERIODIC | Y_WALL | FRAME_XY, X_WALL | Y_PERIODIC])
+@pytest.mark.parametrize("size", SIZES + [(257, 9), (384, 5), (1, 1)],
+                         ids=[f"{w}x{h}" for w, h in SIZES + [(257, 9), (384, 5), (1, 1)]])
+@pytest.mark.parametrize("tile", [(2, 4), (4, 4), (8, 2)])
+def test_strict_f32_periodic_edges_without_solids(gpu, flags, size, tile):
+    """Tiles at periodic edges (incl. partial last tiles) take the interior
+    path with wrapped rows/columns; bit-exact against the oracle."""
+    w, h = size
+    f0 = random_state(w, h, np.float32, seed=w * 7 + h)
+    kw = dict(tau=0.75, flags=flags, force=(1e-5, 3e-6))
+    ref = oracle.step(f0, 6, **kw)
+    f, *_ = gpu_run(f0, 6, tile=tile, **kw)
+    assert np.array_equal(f, ref)
+
+
 @pytest.mark.parametrize("tile", [(4, 1), (4, 4), (4, 8), (8, 1), (8, 3), (8, 8)])
 @pytest.mark.parametrize("flags", [0, X_PERIODIC | Y_WALL | SOLID_HALFWAY | FRAME_XY,
                                    X_PERIODIC | Y_PERIODIC])
