@@ -61,6 +61,11 @@ def parse_args():
     p.add_argument("--no-accuracy", action="store_true")
     p.add_argument("--strict", action="store_true",
                    help="time the reference operation order instead of LBM_FAST")
+    p.add_argument("--no-batch", action="store_true", help="skip the 512-lattice batch")
+    p.add_argument("--batch-steps", type=int, default=2000)
+    p.add_argument("--no-large", action="store_true",
+                   help="skip the 16384^2 f16 / 8192^2 f32 comparison")
+    p.add_argument("--large-steps", type=int, default=500)
     return p.parse_args()
 
 
@@ -329,6 +334,8 @@ def run_ours(args):
 
     # e2e through the C ABI with pinned host buffers
     e2e = run_e2e(spec, args, torch, dist)
+    batch = None if args.no_batch or world > 1 else run_batch(args, torch)
+    large = None if args.no_large or world > 1 else run_large(args, torch)
 
     peak, peak_kind = measured_peak_gbs()
     bpc = BYTES_F32 + BYTES_MASK
@@ -373,11 +380,104 @@ def run_ours(args):
             "gpu_launches": args.steps,
             "clocks": clk,
             "cpu_baseline": cpu,
+            "batch": batch,
+            "large": large,
         }
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
     return 0
+
+
+def run_batch(args, torch):
+    """512 independent lattices, sides U[64, 1024], tau U[0.52, 1.0], Taylor-Green
+    or channel initial state by seed, 0-16 obstacles, f32: autotuned tiles,
+    then --batch-steps steps of all lattices timed with CUDA events."""
+    import tempfile
+    from chemsim_gb300 import lbm
+    from chemsim_gb300.workloads import batch_specs
+    specs = batch_specs(512)
+    cells = sum(s.w * s.h for s in specs)
+    b = lbm.Batch(specs, lbm.FRAME_XY | lbm.FAST)
+    for m, sp in zip(b.members, specs):
+        m.init_equilibrium(sp.rho, sp.ux, sp.uy)
+    stream = torch.cuda.Stream()
+    b.set_stream(stream.cuda_stream)
+    cache = os.path.join(tempfile.gettempdir(), "lbm_batch_tiles.json")
+    if os.path.exists(cache):
+        os.unlink(cache)
+    t0 = time.perf_counter()
+    b.autotune(cache)
+    tune_s = time.perf_counter() - t0
+    with open(cache) as fh:
+        tiles = {str(e["class"]): e["V"] for e in json.load(fh)["lbm_batch_autotune"]}
+    b.step(args.warmup)
+    b.synchronize()
+    start = torch.cuda.Event(enable_timing=True)
+    end = torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    b.step(args.batch_steps)
+    end.record(stream)
+    end.synchronize()
+    secs = start.elapsed_time(end) / 1e3
+    health = [m.health() for m in b.members[:8]]
+    b.close()
+    peak, _ = measured_peak_gbs()
+    gbs = (BYTES_F32 + BYTES_MASK) * cells * args.batch_steps / secs / 1e9
+    return {"workload": "512 lattices, sides U[64,1024], tau U[0.52,1.0], TG or channel, 0-16 obstacles, f32",
+            "cells": cells, "steps": args.batch_steps, "mlups": round(cells * args.batch_steps / secs / 1e6, 1),
+            "achieved_gbs": round(gbs, 1), "frac": round(gbs / peak, 4),
+            "ms_per_step": round(secs / args.batch_steps * 1e3, 4), "autotune_s": round(tune_s, 2),
+            "tiles_cells_per_thread_by_width_class": tiles,
+            "launches_per_step": "one per non-empty (tile width, path) list",
+            "stable": all(not h["unstable"] for h in health)}
+
+
+def run_large(args, torch):
+    """16384^2 f16-deviation channel (256 cylinders r U[20,120], tau 0.52, force
+    5e-7) against 8192^2 f32, and the rho/u L2 error of f16 / f32 against
+    f64 on a 1024^2 sub-problem cut from the same geometry (same window of
+    the mask, same tau and force)."""
+    from chemsim_gb300 import lbm
+    from chemsim_gb300.workloads import CHANNEL_FLAGS, circles_mask
+    flags = CHANNEL_FLAGS | lbm.FAST
+    out = {}
+    big = circles_mask(16384, 16384, 256, 20.0, 120.0, seed=5)
+    for name, n, prec, bpc in (("f16dev_16384", 16384, lbm.F16DEV, BYTES_F16 + BYTES_MASK),
+                               ("f32_8192", 8192, lbm.F32, BYTES_F32 + BYTES_MASK)):
+        solid = np.ascontiguousarray(big[:n, :n])
+        lat = lbm.Lattice(n, n, 0.52, prec, flags)       # starts at rest: rho = 1, u = 0
+        lat.set_force(5e-7, 0.0)
+        lat.set_geometry(solid)
+        stream = torch.cuda.Stream()
+        secs = timed_steps(lat, args.large_steps, args.warmup, torch, stream)
+        h = lat.health()
+        lat.close()
+        mlups = n * n * args.large_steps / secs / 1e6
+        out[name] = {"cells": n * n, "steps": args.large_steps, "mlups": round(mlups, 1),
+                     "achieved_gbs": round(bpc * n * n * args.large_steps / secs / 1e9, 1),
+                     "stable": not h["unstable"]}
+    out["f16_speedup_vs_f32"] = round(out["f16dev_16384"]["mlups"] / out["f32_8192"]["mlups"], 3)
+    # accuracy on the 1024^2 window
+    crop = np.ascontiguousarray(big[:1024, :1024])
+    steps = 2000
+    res = {}
+    for prec in (lbm.F64, lbm.F32, lbm.F16DEV):
+        lat = lbm.Lattice(1024, 1024, 0.52, prec, flags)
+        lat.set_force(5e-7, 0.0)
+        lat.set_geometry(crop)
+        lat.step(steps)
+        res[prec] = lat.moments()
+        lat.close()
+    fluid = crop == 0
+    acc = {}
+    for prec, name in ((lbm.F32, "f32"), (lbm.F16DEV, "f16dev")):
+        r, x, y = res[prec]
+        r6, x6, y6 = res[lbm.F64]
+        acc[name] = {"rho_l2": l2_rel(r[fluid], r6[fluid]),
+                     "u_l2": l2_rel(np.stack([x[fluid], y[fluid]]), np.stack([x6[fluid], y6[fluid]]))}
+    out["accuracy_1024_window"] = {"steps": steps, "against": "f64 run of the same kernel", **acc}
+    return out
 
 
 def run_e2e(spec, args, torch, dist):

@@ -385,6 +385,14 @@ template StepArgs<double> lattice_args<double>(const lbm_lattice*, int, bool);
 template StepArgs<float> lattice_args<__half>(const lbm_lattice*, int, bool);
 template StepArgs<float> lattice_args<__nv_bfloat16>(const lbm_lattice*, int, bool);
 
+int lattice_refresh_moments(lbm_lattice* L) {
+    if (L->mom_valid) return LBM_OK;
+    DeviceGuard g(L->dev);
+    if (int rc = LBM_DISPATCH(L, moments_t, L)) return rc;
+    L->mom_valid = true;
+    return LBM_OK;
+}
+
 void lattice_advance(lbm_lattice* L, int nsteps) {
     if (nsteps & 1) L->cur ^= 1;
     for (int k = 0; k < nsteps; ++k) L->time += L->dt;

@@ -47,6 +47,9 @@ StepArgs<typename Store<S>::CT> lattice_args(const lbm_lattice* L, int from, boo
 // buffer parity, State::time, the step count and the moment cache.
 void lattice_advance(lbm_lattice* L, int nsteps);
 
+// Brings L's moment buffers (rho, ux, uy) up to date with its state.
+int lattice_refresh_moments(lbm_lattice* L);
+
 // Records msg for lbm_last_error_string and returns code.
 int lattice_fail(int code, const std::string& msg);
 

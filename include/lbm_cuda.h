@@ -238,6 +238,50 @@ int lbm_batch_set_stream(lbm_batch* batch, void* stream);
  * mode is reused without timing.  steps_per_trial <= 0 selects 24.         */
 int lbm_batch_autotune(lbm_batch* batch, const char* cache_path, int steps_per_trial);
 
+/* ---- learned coarse-grid correction --------------------------------------
+ * No reference counterpart.  A 4-layer 3x3 convolutional network (channels
+ * 4 -> 32 -> 32 -> 32 -> 9, GELU, bf16 weights, f32 accumulation on the
+ * tensor cores) maps a coarse lattice's fields to a correction of its 9
+ * populations.  Tensors passed as float* are device pointers in NCHW f32:
+ * inputs (batch, 4, h, w) = ((rho - 1) * s_rho, ux * s_u, uy * s_u, solid);
+ * outputs / targets (batch, 9, h, w).                                        */
+
+typedef struct lbm_cnn lbm_cnn;
+
+/* h x w images (w a multiple of 128), up to max_batch per call; weights
+ * initialised from splitmix64(seed).                                        */
+int lbm_cnn_create(int h, int w, int max_batch, uint64_t seed, lbm_cnn** out);
+int lbm_cnn_destroy(lbm_cnn* net);
+int lbm_cnn_param_count(lbm_cnn* net, int64_t* n);
+/* All parameters as one f32 host array: per layer l = 0..3 the weights
+ * W[tap = ky*3 + kx][cin][cout] followed by the biases[cout].              */
+int lbm_cnn_get_params(lbm_cnn* net, float* params);
+int lbm_cnn_set_params(lbm_cnn* net, const float* params);
+int lbm_cnn_forward(lbm_cnn* net, const float* in, int batch, float* out);
+/* Mean-squared-error loss against target and its gradient wrt every
+ * parameter (grads: host array of param_count floats, or NULL).            */
+int lbm_cnn_gradients(lbm_cnn* net, const float* in, const float* target, int batch,
+                      float* loss, float* grads);
+/* One Adam step (beta1 0.9, beta2 0.999) on the MSE loss.                  */
+int lbm_cnn_train_step(lbm_cnn* net, const float* in, const float* target, int batch,
+                       float lr, float* loss);
+int lbm_cnn_synchronize(lbm_cnn* net);
+
+/* Fine -> coarse lattice (both f32; coarse sides = fine sides / factor):
+ * coarse populations = f_eq of the block-averaged fine rho and momentum.   */
+int lbm_restrict(lbm_lattice* fine, lbm_lattice* coarse, int factor);
+/* The network input of a lattice as image `image` of a device tensor
+ * (batch, 4, h, w) f32.                                                     */
+int lbm_coarse_features(lbm_lattice* lat, float s_rho, float s_u, int image, float* in);
+/* f_i += d_i - w_i * sum_j d_j with d_i = scale * corr[image][i], on the
+ * fluid cells of an f32 lattice (the correction never changes a cell's mass). */
+int lbm_coarse_apply(lbm_lattice* lat, const float* corr, int image, float scale);
+/* target[image][i] = (f_i(ref) - f_eq_i(rho, j/rho of cur)) / scale for two
+ * f32 lattices (ref holding equilibria, as lbm_restrict writes them): the
+ * population change that moves cur's density and momentum onto ref's and
+ * leaves cur's non-equilibrium part alone.                                  */
+int lbm_coarse_target(lbm_lattice* ref, lbm_lattice* cur, float scale, int image, float* target);
+
 #ifdef __cplusplus
 }
 #endif

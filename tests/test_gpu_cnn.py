@@ -1,0 +1,148 @@
+"""The correction network (tcgen05 convolutions) and the coarse-grid calls
+against the CPU oracles."""
+import numpy as np
+import pytest
+
+import oracle
+from oracle import cnn_oracle as co
+from chemsim_gb300 import lbm
+from chemsim_gb300.lbm import F32, FAST, FRAME_XY, SOLID_HALFWAY, X_PERIODIC, Y_WALL, Lattice
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+from chemsim_gb300.learned import (CorrectionNet, apply_correction, features,  # noqa: E402
+                                   restrict, target)
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(np.asarray(a, np.float64) - b) / max(np.linalg.norm(b), 1e-30))
+
+
+@pytest.fixture(scope="module")
+def small_case():
+    B, H, W = 2, 8, 128
+    rng = np.random.default_rng(0)
+    p = co.init_params(1).astype(np.float32)
+    x = rng.normal(size=(B, 4, H, W)).astype(np.float32)
+    t = (rng.normal(size=(B, 9, H, W)) * 0.1).astype(np.float32)
+    return p, x, t
+
+
+def test_forward_matches_oracle(gpu, small_case):
+    p, x, _ = small_case
+    B, _, H, W = x.shape
+    with CorrectionNet(H, W, B) as net:
+        net.set_params(p)
+        assert np.array_equal(net.get_params(), p)
+        out = torch.empty((B, 9, H, W), device="cuda")
+        net.forward(torch.from_numpy(x).cuda(), out)
+        ref, _ = co.forward(p.astype(np.float64), x.astype(np.float64))
+        # bf16 activations: the oracle rounds at the same points; sums differ
+        # in order only (f32 on the tensor cores vs f64)
+        assert _rel(out.cpu().numpy(), ref) < 2e-3
+
+
+def test_gradients_match_oracle(gpu, small_case):
+    p, x, t = small_case
+    B, _, H, W = x.shape
+    with CorrectionNet(H, W, B) as net:
+        net.set_params(p)
+        loss, g = net.gradients(torch.from_numpy(x).cuda(), torch.from_numpy(t).cuda())
+        lref, gref = co.gradients(p.astype(np.float64), x.astype(np.float64), t.astype(np.float64))
+        assert abs(loss - lref) <= 1e-3 * lref
+        k = 0
+        for ci, cout in zip(co.CIN, co.COUT):
+            for n in (9 * ci * cout, cout):
+                assert _rel(g[k:k + n], gref[k:k + n]) < 5e-3, k
+                k += n
+
+
+def test_training_reduces_loss(gpu):
+    B, H, W = 2, 16, 128
+    rng = np.random.default_rng(4)
+    x = rng.normal(size=(B, 4, H, W)).astype(np.float32)
+    # a target the network can represent: a smoothed function of the input
+    t = np.tanh(x[:, :3].mean(axis=1, keepdims=True)).repeat(9, axis=1).astype(np.float32) * 0.3
+    with CorrectionNet(H, W, B, seed=7) as net:
+        xd, td = torch.from_numpy(x).cuda(), torch.from_numpy(t).cuda()
+        first = net.train_step(xd, td, 1e-3)
+        for _ in range(150):
+            last = net.train_step(xd, td, 1e-3)
+        assert last < 0.3 * first
+
+
+def test_batch_bounds_checked(gpu):
+    with CorrectionNet(8, 128, 2) as net:
+        x = torch.zeros((3, 4, 8, 128), device="cuda")
+        out = torch.zeros((3, 9, 8, 128), device="cuda")
+        with pytest.raises(lbm.LBMError):
+            net.forward(x, out)
+    with pytest.raises(lbm.LBMError):
+        CorrectionNet(8, 100, 1)          # width must be a multiple of 128
+
+
+def _channel(w, h, seed):
+    from chemsim_gb300.workloads import channel_spec
+    return channel_spec(w, n_obstacles=3, r_lo=4, r_hi=9, force=1e-5, seed=seed, h=h)
+
+
+def test_restrict_matches_block_average(gpu):
+    spec = _channel(128, 64, 3)
+    flags = X_PERIODIC | Y_WALL | SOLID_HALFWAY | FRAME_XY | FAST
+    with Lattice(128, 64, 0.6, F32, flags) as fine, Lattice(32, 16, 0.525, F32, flags) as coarse:
+        fine.set_force(*spec.force)
+        fine.set_geometry(spec.solid)
+        fine.init_equilibrium(spec.rho, spec.ux, spec.uy)
+        fine.step(50)
+        rho, ux, uy = fine.moments()
+        coarse.set_force(4 * spec.force[0], 0.0)
+        restrict(fine, coarse, 4)
+        got = coarse.get_populations()
+        fl = (spec.solid == 0).reshape(16, 4, 32, 4)
+        r4 = rho.reshape(16, 4, 32, 4).astype(np.float64)
+        n = fl.sum(axis=(1, 3))
+        sr = (r4 * fl).sum(axis=(1, 3))
+        rc = np.where(n > 0, sr / np.maximum(n, 1), 1.0)
+        jx = (r4 * ux.reshape(16, 4, 32, 4) * fl).sum(axis=(1, 3))
+        jy = (r4 * uy.reshape(16, 4, 32, 4) * fl).sum(axis=(1, 3))
+        vx = np.where(sr > 0, jx / np.where(sr > 0, sr, 1), 0) + np.where(n > 0, 0.5 * 4 * spec.force[0] / rc, 0)
+        vy = np.where(sr > 0, jy / np.where(sr > 0, sr, 1), 0)
+        ref = oracle.equilibrium(rc.astype(np.float32), vx.astype(np.float32), vy.astype(np.float32))
+        assert np.max(np.abs(got - ref)) < 2e-6
+
+
+def test_features_apply_target(gpu):
+    spec = _channel(128, 32, 5)
+    flags = X_PERIODIC | Y_WALL | SOLID_HALFWAY | FRAME_XY | FAST
+    with Lattice(128, 32, 0.6, F32, flags) as a, Lattice(128, 32, 0.6, F32, flags) as b:
+        for lat in (a, b):
+            lat.set_geometry(spec.solid)
+        rng = np.random.default_rng(9)
+        rho = (1 + 0.01 * rng.normal(size=(32, 128))).astype(np.float32)
+        ux = (0.01 * rng.normal(size=(32, 128))).astype(np.float32)
+        uy = (0.01 * rng.normal(size=(32, 128))).astype(np.float32)
+        a.init_equilibrium(rho, ux, uy)
+        b.init_equilibrium(np.ones_like(rho), ux * 0, uy * 0)
+        x = torch.zeros((2, 4, 32, 128), device="cuda")
+        features(a, x, 1, 100.0, 50.0)
+        r, vx, vy = a.moments()
+        solid = spec.solid.astype(bool)
+        xs = x[1].cpu().numpy()
+        np.testing.assert_allclose(xs[0], np.where(solid, 0, (r - 1) * 100), rtol=1e-6, atol=1e-6)
+        np.testing.assert_allclose(xs[1], np.where(solid, 0, vx * 50), rtol=1e-6, atol=1e-7)
+        np.testing.assert_array_equal(xs[3], solid.astype(np.float32))
+        assert float(x[0].abs().sum()) == 0.0
+        t = torch.zeros((1, 9, 32, 128), device="cuda")
+        target(a, b, t, 0, 1e-3)
+        fa, fb = a.get_populations(), b.get_populations()
+        # b holds equilibria, so f_eq of its own moments is fb itself
+        np.testing.assert_allclose(t[0].cpu().numpy(), (fa - fb) / 1e-3, rtol=1e-5, atol=1e-3)
+        apply_correction(b, t, 0, 1e-3)
+        got = b.get_populations()
+        w = np.array([16, 4, 4, 4, 4, 1, 1, 1, 1], np.float64)[:, None, None] / 36
+        d = (fa - fb).astype(np.float64)
+        exp = np.where(solid[None], fb, fb + d - w * d.sum(axis=0, keepdims=True))
+        np.testing.assert_allclose(got, exp, rtol=0, atol=3e-7)
+        # mass per fluid cell unchanged by the correction
+        np.testing.assert_allclose(got.sum(axis=0), fb.sum(axis=0), rtol=0, atol=1e-6)
