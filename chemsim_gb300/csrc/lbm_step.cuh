@@ -23,6 +23,7 @@
 #pragma once
 
 #include "lbm_common.cuh"
+#include "lbm_pair.cuh"
 
 namespace lbmk {
 
@@ -372,6 +373,40 @@ __device__ __forceinline__ void collide_domain(const Consts<CT>& c, const CT (&g
     else collide_cell<FAST>(c, g, out);
 }
 
+// Collides a thread's V cells in place.  f32 collision arithmetic in fast or
+// deviation form takes the cells in pairs on the packed f32x2 instructions.
+#ifndef LBM_PAIRED
+#define LBM_PAIRED 1
+#endif
+template <class S, int V, bool FAST>
+__device__ __forceinline__ void collide_cells(const Consts<typename Store<S>::CT>& c,
+                                              typename Store<S>::CT (&f)[9][V]) {
+    using CT = typename Store<S>::CT;
+    constexpr bool paired = LBM_PAIRED && sizeof(CT) == 4 && V % 2 == 0 && (FAST || Store<S>::DEV);
+    if constexpr (paired) {
+#pragma unroll
+        for (int k = 0; k < V; k += 2) {
+            float2 g[9], o[9];
+#pragma unroll
+            for (int i = 0; i < 9; ++i) g[i] = make_float2(f[i][k], f[i][k + 1]);
+            if constexpr (Store<S>::DEV) collide_dev_x2(c, g, o);
+            else collide_fast_x2(c, g, o);
+#pragma unroll
+            for (int i = 0; i < 9; ++i) { f[i][k] = o[i].x; f[i][k + 1] = o[i].y; }
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < V; ++k) {
+            CT g[9], o[9];
+#pragma unroll
+            for (int i = 0; i < 9; ++i) g[i] = f[i][k];
+            collide_domain<S, FAST>(c, g, o);
+#pragma unroll
+            for (int i = 0; i < 9; ++i) f[i][k] = o[i];
+        }
+    }
+}
+
 // Writes the V collided cells of a thread and, when requested, their moments
 // (computed from the stored, i.e. encoded, values).
 template <class S, int V, bool FAST>
@@ -450,15 +485,7 @@ __device__ __forceinline__ void step_interior(const StepArgs<typename Store<S>::
 #pragma unroll
         for (int k = 0; k < V; ++k) f[i][k] = v[k];
     }
-#pragma unroll
-    for (int k = 0; k < V; ++k) {
-        CT g[9], o[9];
-#pragma unroll
-        for (int i = 0; i < 9; ++i) g[i] = f[i][k];
-        collide_domain<S, FAST>(a.c, g, o);
-#pragma unroll
-        for (int i = 0; i < 9; ++i) f[i][k] = o[i];
-    }
+    collide_cells<S, V, FAST>(a.c, f);
     S enc[9][V];
 #pragma unroll
     for (int i = 0; i < 9; ++i) ST::enc_vec_dom(f[i], enc[i]);
@@ -530,15 +557,7 @@ __device__ __forceinline__ void step_interior_wrap(const StepArgs<typename Store
 #pragma unroll
         for (int k = 0; k < V; ++k) f[i][k] = v[k];
     }
-#pragma unroll
-    for (int k = 0; k < V; ++k) {
-        CT g[9], o[9];
-#pragma unroll
-        for (int i = 0; i < 9; ++i) g[i] = f[i][k];
-        collide_domain<S, FAST>(a.c, g, o);
-#pragma unroll
-        for (int i = 0; i < 9; ++i) f[i][k] = o[i];
-    }
+    collide_cells<S, V, FAST>(a.c, f);
     S enc[9][V];
 #pragma unroll
     for (int i = 0; i < 9; ++i) ST::enc_vec_dom(f[i], enc[i]);
@@ -719,15 +738,7 @@ __device__ __forceinline__ void step_general(const StepArgs<typename Store<S>::C
 
     // ---- phase D: collide and write ---------------------------------------
     S enc[9][V];
-#pragma unroll
-    for (int k = 0; k < V; ++k) {
-        CT g[9], o[9];
-#pragma unroll
-        for (int i = 0; i < 9; ++i) g[i] = f[i][k];
-        collide_domain<S, FAST>(a.c, g, o);
-#pragma unroll
-        for (int i = 0; i < 9; ++i) f[i][k] = o[i];
-    }
+    collide_cells<S, V, FAST>(a.c, f);
 #pragma unroll
     for (int i = 0; i < 9; ++i) ST::enc_vec_dom(f[i], enc[i]);
 
@@ -753,8 +764,17 @@ __device__ __forceinline__ void step_general(const StepArgs<typename Store<S>::C
 // overlaps the rest; the remaining blocks cover every (row, tile) in row-major
 // order and run the interior path, leaving tiles flagged 1 to the list.
 // Without tile flags, every tile takes the general path.
+// Resident blocks of 256 threads the register allocation is sized for (V <= 4).
+#ifndef LBM_STEP_MIN_BLOCKS
+#define LBM_STEP_MIN_BLOCKS 3
+#endif
+#ifndef LBM_STEP_MIN_BLOCKS_16
+#define LBM_STEP_MIN_BLOCKS_16 3
+#endif
 template <class S, int V, int FRAME, bool FAST>
-__global__ void __launch_bounds__(256, (sizeof(typename Store<S>::CT) == 4 && V <= 4) ? 3 : 1)
+__global__ void __launch_bounds__(256, (sizeof(typename Store<S>::CT) == 4 && V <= 4)
+                                           ? (sizeof(S) == 2 ? LBM_STEP_MIN_BLOCKS_16 : LBM_STEP_MIN_BLOCKS)
+                                           : 1)
 lbm_step_kernel(const StepArgs<typename Store<S>::CT> a) {
     const int rows = blockDim.y;
     const int gblocks = a.tflags != nullptr ? (a.ngtiles + rows - 1) / rows : 0;
