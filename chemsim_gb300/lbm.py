@@ -27,6 +27,9 @@ from ._lib import (BF16DEV, COLLISION_BGK, COLLISION_TRT, F16DEV, F32, F64,  # n
                    SOLID_HALFWAY, X_PERIODIC, X_WALL, X_ZEROPAD, Y_PERIODIC,
                    Y_WALL, Y_ZEROPAD, LBMError, LBMHealth, check)
 
+# render modes (src/main.rs:158-173 DisplayMode)
+RENDER_DENSITY, RENDER_SPEED, RENDER_VELOCITY, RENDER_MOMENTUM = 0, 1, 2, 3
+
 # src/lbm.rs:205-227 (as f32)
 WEIGHTS = tuple(np.float32(n) / np.float32(36.0) for n in (16, 4, 4, 4, 4, 1, 1, 1, 1))
 VELOCITIES = ((0, 0), (1, 0), (0, 1), (-1, 0), (0, -1), (1, 1), (-1, 1), (-1, -1), (1, -1))
@@ -142,6 +145,19 @@ class Lattice:
     def moments_to_device(self, rho_ptr: int, ux_ptr: int, uy_ptr: int):
         check(self._lib.lbm_read_moments(self._h, ctypes.c_void_p(rho_ptr),
                                          ctypes.c_void_p(ux_ptr), ctypes.c_void_p(uy_ptr), 1))
+
+    def render(self, mode: int = 0, geometry_overlay: bool = True) -> np.ndarray:
+        """RGBA8 image (h, w, 4) of a moment field coloured as src/render.rs
+        does (mode: RENDER_DENSITY, RENDER_SPEED, RENDER_VELOCITY,
+        RENDER_MOMENTUM)."""
+        img = np.empty((self.h, self.w, 4), dtype=np.uint8)
+        check(self._lib.lbm_render(self._h, int(mode), int(bool(geometry_overlay)),
+                                   img.ctypes.data_as(ctypes.c_void_p), 0))
+        return img
+
+    def render_to_device(self, rgba_ptr: int, mode: int = 0, geometry_overlay: bool = True):
+        check(self._lib.lbm_render(self._h, int(mode), int(bool(geometry_overlay)),
+                                   ctypes.c_void_p(rgba_ptr), 1))
 
     def health(self) -> dict:
         hs = LBMHealth()
