@@ -520,6 +520,7 @@ int lbm_destroy(lbm_lattice* L) {
         if (L->solid) cudaFree(L->solid);
         if (L->staging) cudaFree(L->staging);
         if (L->health) cudaFree(L->health);
+        if (L->render) cudaFree(L->render);
         if (L->tflags) cudaFree(L->tflags);
         if (L->gtiles) cudaFree(L->gtiles);
         if (L->own) cudaStreamDestroy(L->own);

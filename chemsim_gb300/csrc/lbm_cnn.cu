@@ -391,7 +391,8 @@ struct lbm_cnn {
     double* loss_partial = nullptr;
     int* err = nullptr;
     int dw_blocks = 0;
-    cudaStream_t stream = nullptr;
+    cudaStream_t stream = nullptr;     // where every call issues its work
+    cudaStream_t own = nullptr;        // created with the net; used when no stream is set
     int dev = 0;
 };
 
@@ -560,8 +561,9 @@ int lbm_cnn_create(int h, int w, int max_batch, uint64_t seed, lbm_cnn** out) {
         const double lim = std::sqrt(6.0 / (9.0 * kCin[l])) * (l == kLayers - 1 ? 0.1 : 1.0);
         for (int k = 0; k < 9 * kCin[l] * kCout[l]; ++k) p[N->off_w[l] + k] = float((2.0 * next() - 1.0) * lim);
     }
-    cudaError_t e = cudaStreamCreateWithFlags(&N->stream, cudaStreamNonBlocking);
+    cudaError_t e = cudaStreamCreateWithFlags(&N->own, cudaStreamNonBlocking);
     if (e != cudaSuccess) return cleanup(cfail(LBM_ERR_CUDA, cudaGetErrorString(e)));
+    N->stream = N->own;
     auto alloc = [&](void** ptr, size_t bytes) -> int {
         cudaError_t r = cudaMalloc(ptr, bytes);
         if (r != cudaSuccess) {
@@ -620,7 +622,7 @@ int lbm_cnn_destroy(lbm_cnn* N) {
     }
     for (auto* g : N->gbuf)
         if (g) cudaFree(g);
-    if (N->stream) cudaStreamDestroy(N->stream);
+    if (N->own) cudaStreamDestroy(N->own);
     delete N;
     return LBM_OK;
 }
@@ -696,6 +698,13 @@ int lbm_cnn_train_step(lbm_cnn* N, const float* in_dev, const float* target_dev,
                                                                   1e-8f, c1, c2);
     CNN_CUDA(cudaGetLastError());
     if (int rc = repack(N)) return rc;
+    return LBM_OK;
+}
+
+int lbm_cnn_set_stream(lbm_cnn* N, void* stream) {
+    if (!N) return cfail(LBM_ERR_INVALID_ARGUMENT, "null argument");
+    CNN_CUDA(cudaStreamSynchronize(N->stream));
+    N->stream = stream ? static_cast<cudaStream_t>(stream) : N->own;
     return LBM_OK;
 }
 

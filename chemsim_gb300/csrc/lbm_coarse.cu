@@ -1,7 +1,8 @@
 // lbm_coarse.cu — the lattice side of the learned coarse-grid correction:
 // restriction of a fine lattice onto a coarser one, the correction network's
 // input features, the application of its population correction and the
-// training target (restricted fine minus evolved coarse populations).
+// training target (the population change that moves the coarse velocity
+// onto the restricted fine one).
 // No reference counterpart.
 #include <string>
 
@@ -33,57 +34,75 @@ __global__ void features_kernel(const float* __restrict__ rho, const float* __re
     }
 }
 
-// f_i += scale * corr[b][i] on fluid cells of an f32 lattice, projected so
-// that the cell's mass does not change.
+// Raw density and velocity j / rho of a stored f32 cell.
+__device__ __forceinline__ void raw_moments(const float (&f)[9], float& rho, float& ux, float& uy) {
+    rho = ((f[0] + f[1]) + (f[2] + f[3])) + ((f[4] + f[5]) + (f[6] + f[7])) + f[8];
+    const float jx = (f[1] - f[3]) + (f[5] - f[6]) + (f[8] - f[7]);
+    const float jy = (f[2] - f[4]) + (f[5] + f[6]) - (f[7] + f[8]);
+    ux = jx / rho;
+    uy = jy / rho;
+}
+
+// Population correction of the fluid cells of an f32 lattice: d_i = scale *
+// corr[b][i] (clamped to +-max_abs when max_abs > 0), applied as
+// f_i += d_i - w_i sum_j d_j so that the cell's mass does not change.
 __global__ void apply_correction_kernel(float* __restrict__ f, int64_t plane, int pitch,
                                         const uint8_t* __restrict__ solid, int mpitch, int H, int W,
-                                        const float* __restrict__ corr, int b, float scale) {
+                                        const float* __restrict__ corr, int b, float scale,
+                                        float max_abs) {
     const int64_t n = int64_t(H) * W;
+    const float w[9] = {16.f / 36.f, 4.f / 36.f, 4.f / 36.f, 4.f / 36.f, 4.f / 36.f,
+                        1.f / 36.f, 1.f / 36.f, 1.f / 36.f, 1.f / 36.f};
     for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < n;
          e += int64_t(gridDim.x) * blockDim.x) {
         const int y = int(e / W), x = int(e % W);
         if (solid != nullptr && solid[int64_t(y) * mpitch + x]) continue;
         const int64_t o = int64_t(y) * pitch + x;
-        // the correction is projected to zero mass change: d_i - w_i sum(d)
         float d[9], sum = 0.f;
 #pragma unroll
         for (int i = 0; i < 9; ++i) {
-            d[i] = scale * corr[((int64_t(b) * 9 + i) * H + y) * W + x];
+            d[i] = scale * corr[(int64_t(b) * 9 + i) * n + e];
+            if (max_abs > 0.f) d[i] = fminf(fmaxf(d[i], -max_abs), max_abs);
             sum += d[i];
         }
-        const float w[9] = {16.f / 36.f, 4.f / 36.f, 4.f / 36.f, 4.f / 36.f, 4.f / 36.f,
-                            1.f / 36.f, 1.f / 36.f, 1.f / 36.f, 1.f / 36.f};
 #pragma unroll
         for (int i = 0; i < 9; ++i) f[i * plane + o] += d[i] - w[i] * sum;
     }
 }
 
-// target[b][i] = (ref_i - f_eq_i(rho, j / rho of cur)) / scale: the
-// population change that moves cur's density and momentum onto ref's while
-// leaving cur's non-equilibrium part alone (ref holds equilibria, written by
-// the restriction).
-__global__ void population_diff_kernel(const float* __restrict__ ref, const float* __restrict__ cur,
-                                       int64_t plane, int pitch, int H, int W, float inv_scale,
-                                       int b, float* __restrict__ target, Consts<float> c) {
+// target[b][i] = (f_eq_i(rho_cur, u_ref) - f_eq_i(rho_cur, u_cur)) / scale
+// with u = j / rho of the stored states (ref holds equilibria, written by the
+// restriction); zero on solid cells.  The target moves cur's velocity onto
+// ref's and changes neither its density nor its non-equilibrium part.
+__global__ void velocity_shift_kernel(const float* __restrict__ ref, const float* __restrict__ cur,
+                                      int64_t plane, int pitch, const uint8_t* __restrict__ solid,
+                                      int mpitch, int H, int W, float inv_scale, int b,
+                                      float* __restrict__ target, Consts<float> c) {
     const int64_t n = int64_t(H) * W;
     for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < n;
          e += int64_t(gridDim.x) * blockDim.x) {
         const int y = int(e / W), x = int(e % W);
         const int64_t o = int64_t(y) * pitch + x;
-        float f[9];
+        float* t = target + int64_t(b) * 9 * n + e;
+        if (solid != nullptr && solid[int64_t(y) * mpitch + x]) {
 #pragma unroll
-        for (int i = 0; i < 9; ++i) f[i] = cur[i * plane + o];
-        float rho, jx, jy;
-        {
-            Consts<float> c0 = c;
-            c0.force = 0;                          // raw momentum j = sum f c
-            cell_moments<false>(c0, f, rho, jx, jy);
+            for (int i = 0; i < 9; ++i) t[i * n] = 0.f;
+            continue;
         }
-        float feq[9];
-        equilibrium_strict<float>(c, rho, jx, jy, feq);
+        float fr[9], fc[9];
 #pragma unroll
-        for (int i = 0; i < 9; ++i)
-            target[((int64_t(b) * 9 + i) * H + y) * W + x] = (ref[i * plane + o] - feq[i]) * inv_scale;
+        for (int i = 0; i < 9; ++i) {
+            fr[i] = ref[i * plane + o];
+            fc[i] = cur[i * plane + o];
+        }
+        float rr, rx, ry, rc, cx, cy;
+        raw_moments(fr, rr, rx, ry);
+        raw_moments(fc, rc, cx, cy);
+        float e0[9], e1[9];
+        equilibrium_strict<float>(c, rc, cx, cy, e0);
+        equilibrium_strict<float>(c, rc, rx, ry, e1);
+#pragma unroll
+        for (int i = 0; i < 9; ++i) t[i * n] = (e1[i] - e0[i]) * inv_scale;
     }
 }
 
@@ -180,12 +199,13 @@ int lbm_coarse_features(lbm_lattice* lat, float s_rho, float s_u, int image, flo
     return LBM_OK;
 }
 
-int lbm_coarse_apply(lbm_lattice* lat, const float* corr, int image, float scale) {
-    if (!f32_lattice(lat) || !corr || image < 0)
-        return kfail(LBM_ERR_INVALID_ARGUMENT, "need an f32 lattice and a correction");
+int lbm_coarse_apply(lbm_lattice* lat, const float* corr, int image, float scale, float max_abs) {
+    if (!f32_lattice(lat) || !corr || image < 0 || !(max_abs >= 0.f))
+        return kfail(LBM_ERR_INVALID_ARGUMENT, "need an f32 lattice, a correction and max_abs >= 0");
     apply_correction_kernel<<<grid_of(int64_t(lat->w) * lat->h, 256), 256, 0, lat->stream>>>(
         static_cast<float*>(lat->buf[lat->cur]), lat->plane, lat->pitch,
-        lat->has_solid ? lat->solid : nullptr, lat->mpitch, lat->h, lat->w, corr, image, scale);
+        lat->has_solid ? lat->solid : nullptr, lat->mpitch, lat->h, lat->w, corr, image, scale,
+        max_abs);
     CO_CUDA(cudaGetLastError());
     lat->mom_valid = false;
     return LBM_OK;
@@ -196,10 +216,10 @@ int lbm_coarse_target(lbm_lattice* ref, lbm_lattice* cur, float scale, int image
         return kfail(LBM_ERR_INVALID_ARGUMENT, "need two f32 lattices, a target and scale > 0");
     if (ref->w != cur->w || ref->h != cur->h) return kfail(LBM_ERR_INVALID_ARGUMENT, "size mismatch");
     CO_CUDA(cudaStreamSynchronize(ref->stream));
-    population_diff_kernel<<<grid_of(int64_t(cur->w) * cur->h, 256), 256, 0, cur->stream>>>(
+    velocity_shift_kernel<<<grid_of(int64_t(cur->w) * cur->h, 256), 256, 0, cur->stream>>>(
         static_cast<const float*>(ref->buf[ref->cur]), static_cast<const float*>(cur->buf[cur->cur]),
-        cur->plane, cur->pitch, cur->h, cur->w, 1.f / scale, image, target,
-        lattice_args<float>(cur, cur->cur, false).c);
+        cur->plane, cur->pitch, cur->has_solid ? cur->solid : nullptr, cur->mpitch, cur->h, cur->w,
+        1.f / scale, image, target, lattice_args<float>(cur, cur->cur, false).c);
     CO_CUDA(cudaGetLastError());
     return LBM_OK;
 }

@@ -20,6 +20,8 @@ struct lbm_lattice {
     void* staging = nullptr;
     size_t staging_bytes = 0;
     lbmk::HealthPartial* health = nullptr;  // kHealthBlocks partials + 1 result
+    void* render = nullptr;               // colour-map scratch (stats, host-bound image)
+    size_t render_bytes = 0;
     uint8_t* tflags = nullptr;            // h x ceil(w / 32) bytes
     int ntiles = 0;
     uint32_t* gtiles = nullptr;           // list of flagged tiles

@@ -77,6 +77,10 @@ class CorrectionNet:
                                            float(lr), ctypes.byref(loss)))
         return float(loss.value)
 
+    def set_stream(self, stream_ptr: int | None):
+        """Issue the net's work on this cudaStream_t (None: its own stream)."""
+        check(self._lib.lbm_cnn_set_stream(self._n, ctypes.c_void_p(stream_ptr or 0)))
+
     def synchronize(self):
         check(self._lib.lbm_cnn_synchronize(self._n))
 
@@ -89,8 +93,8 @@ def features(lat, x, image: int, s_rho: float, s_u: float):
     check(_lib.load().lbm_coarse_features(lat.handle, float(s_rho), float(s_u), int(image), _ptr(x)))
 
 
-def apply_correction(lat, corr, image: int, scale: float):
-    check(_lib.load().lbm_coarse_apply(lat.handle, _ptr(corr), int(image), float(scale)))
+def apply_correction(lat, corr, image: int, scale: float, max_abs: float = 0.0):
+    check(_lib.load().lbm_coarse_apply(lat.handle, _ptr(corr), int(image), float(scale), float(max_abs)))
 
 
 def target(ref, cur, t, image: int, scale: float):
@@ -119,21 +123,24 @@ class CorrectionConfig:
     r_hi: float = 32.0
     k: int = 8                    # coarse steps between corrections
     train_lattices: int = 8
-    pairs: int = 4000
+    pairs: int = 5000             # horizon_fine / (k * factor) intervals x train_lattices
     horizon_fine: int = 20000     # fine-equivalent steps of the evaluation
     batch: int = 8
-    buffer: int = 512
-    iters_per_round: int = 2
-    final_iters: int = 400
+    buffer: int = 2500            # pairs kept for training (evenly thinned)
+    final_iters: int = 3000       # Adam iterations
     lr: float = 1e-3
-    s_rho: float = 1000.0
+    s_rho: float = 0.0             # density input off: its acoustic part is noise here
     s_u: float = 100.0
     s_out: float = 1e-4
     seed: int = 11
     eval_seed: int = 9999
     checkpoints: int = 10
-    check_every: int = 64
     mass_tolerance: float = 1e-3
+    gain: float = 1.0             # fraction of the predicted correction applied
+    clip: float = 4.0             # |d_i| limit in RMS of the training targets (0: none)
+    data_policy: str = "none"     # first data pass: "none" (coarse-only run) or "teacher"
+    onpolicy_passes: int = 0      # data passes with the network's own corrections applied
+    onpolicy_iters: int = 1500
     extra: dict = field(default_factory=dict)
 
     @property
@@ -170,163 +177,259 @@ def _l2(cx, cy, rx, ry, mask):
     return float(num / max(den, 1e-300))
 
 
-def run_correction_experiment(cfg: CorrectionConfig, log=None) -> dict:
-    """Generates snapshot pairs with the batched fine LBM, trains the network
-    on the GPU, and judges coarse-only and coarse-plus-correction runs against
-    the fine run of a held-out geometry.  Returns a result dict."""
+def _coarse_specs(cfg: CorrectionConfig, seeds):
+    from .workloads import LatticeSpec, channel_spec
+    fine = [channel_spec(cfg.fine, tau=cfg.tau_fine, n_obstacles=cfg.n_obstacles, r_lo=cfg.r_lo,
+                         r_hi=cfg.r_hi, force=cfg.force_fine, seed=s) for s in seeds]
+    coarse = [LatticeSpec(cfg.coarse, cfg.coarse, cfg.tau_coarse, f.flags,
+                          force=(cfg.force_fine * cfg.factor, 0.0),
+                          solid=coarse_geometry(f.solid, cfg.factor)) for f in fine]
+    return fine, coarse
+
+
+def train_correction(cfg: CorrectionConfig, stream, log=None):
+    """Snapshot pairs from the batched fine LBM, then Adam on the GPU.
+
+    Every lattice pair runs side by side from rest: each interval the coarse
+    lattice takes k steps and the fine one k * factor; the restricted fine
+    state is the reference and the pair (features of the coarse state, the
+    population change that moves its velocity onto the reference's) is
+    stored.  In the first pass that change itself is then applied to the
+    coarse lattice (teacher forcing); in each later pass the network's own
+    prediction is applied instead (the states a corrected run visits, so the
+    network learns to pull its own drift back), the new pairs replace the
+    buffer and training continues.
+
+    Returns (net, s_eff, info): the applied correction is net output * s_eff.
+    """
     import torch
     from . import lbm
-    from .workloads import CHANNEL_FLAGS, channel_spec
     say = log or (lambda *a: None)
-    flags = CHANNEL_FLAGS | lbm.FAST
-    nf, nc, fac = cfg.fine, cfg.coarse, cfg.factor
-    force_c = cfg.force_fine * fac
+    nc, fac, nl = cfg.coarse, cfg.factor, cfg.train_lattices
     dev = torch.device("cuda")
-    res = {"config": {k: v for k, v in cfg.__dict__.items() if k != "extra"},
-           "tau_coarse": cfg.tau_coarse, "force_coarse": force_c}
-
-    # ---- snapshot pairs from the batched fine LBM, online training ---------
-    specs = [channel_spec(nf, tau=cfg.tau_fine, n_obstacles=cfg.n_obstacles, r_lo=cfg.r_lo,
-                          r_hi=cfg.r_hi, force=cfg.force_fine, seed=cfg.seed + i)
-             for i in range(cfg.train_lattices)]
-    cmasks = [coarse_geometry(s.solid, fac) for s in specs]
-    from .workloads import LatticeSpec
-    cspecs = [LatticeSpec(nc, nc, cfg.tau_coarse, s.flags, force=(force_c, 0.0), solid=m)
-              for s, m in zip(specs, cmasks)]
-    fine_b = lbm.Batch(specs, lbm.FRAME_XY | lbm.FAST)
-    cur_b = lbm.Batch(cspecs, lbm.FRAME_XY | lbm.FAST)
+    specs, cspecs = _coarse_specs(cfg, [cfg.seed + i for i in range(nl)])
     refs = []
-    for m in cmasks:
-        r = lbm.Lattice(nc, nc, cfg.tau_coarse, lbm.F32, flags)
-        r.set_force(force_c, 0.0)
-        r.set_geometry(m)
+    for cs in cspecs:
+        r = lbm.Lattice(nc, nc, cfg.tau_coarse, lbm.F32, cs.flags | lbm.FAST)
+        r.set_force(*cs.force)
+        r.set_geometry(cs.solid)
+        r.set_stream(stream.cuda_stream)
         refs.append(r)
-    net = CorrectionNet(nc, nc, max(cfg.batch, 1), seed=cfg.seed)
-    xb = torch.zeros((cfg.buffer, 4, nc, nc), device=dev)
-    tb = torch.zeros((cfg.buffer, 9, nc, nc), device=dev)
-    rounds = max(1, cfg.pairs // cfg.train_lattices)
-    spacing = max(cfg.k * fac, (cfg.horizon_fine * cfg.train_lattices) // max(cfg.pairs, 1))
+    net = CorrectionNet(nc, nc, max(cfg.batch, nl), seed=cfg.seed)
+    net.set_stream(stream.cuda_stream)
+    rounds = max(1, cfg.pairs // nl)
+    keep = max(1, (rounds * nl + cfg.buffer - 1) // cfg.buffer)
+    nbuf = min(cfg.buffer, rounds * nl)
     rng = np.random.default_rng(cfg.seed)
-    filled, slot, losses = 0, 0, []
+    losses, passes = [], []
     t_gen = t_train = 0.0
-    for rd in range(rounds):
+
+    with torch.cuda.stream(stream):
+        xb = torch.zeros((nbuf, 4, nc, nc), device=dev)
+        tb = torch.zeros((nbuf, 9, nc, nc), device=dev)
+        xs = torch.zeros((nl, 4, nc, nc), device=dev)
+        ts = torch.zeros((nl, 9, nc, nc), device=dev)
+        os_ = torch.zeros((nl, 9, nc, nc), device=dev)
+        stream.synchronize()
+
+        def generate(scale, policy):
+            """One pass over the training horizon; fills the buffer (targets
+            in units of `scale`).  policy "teacher": the target itself is
+            applied; "none": nothing is applied (the coarse-only run, whose
+            accumulated gap to the fine run becomes the target); a number:
+            the network's correction with that gain."""
+            fine_b = lbm.Batch(specs, lbm.FRAME_XY | lbm.FAST)
+            cur_b = lbm.Batch(cspecs, lbm.FRAME_XY | lbm.FAST)
+            fine_b.set_stream(stream.cuda_stream)
+            cur_b.set_stream(stream.cuda_stream)
+            for m, c in zip(fine_b.members, cur_b.members):
+                restrict(m, c, fac)
+            slot = count = 0
+            for _ in range(rounds):
+                cur_b.step(cfg.k)
+                fine_b.step(cfg.k * fac)
+                for i, (m, c, r) in enumerate(zip(fine_b.members, cur_b.members, refs)):
+                    restrict(m, r, fac)
+                    features(c, xs, i, cfg.s_rho, cfg.s_u)
+                    target(r, c, ts, i, scale)
+                if not isinstance(policy, str):
+                    net.forward(xs, os_)
+                for i, c in enumerate(cur_b.members):
+                    if policy == "teacher":
+                        apply_correction(c, ts, i, scale)
+                    elif not isinstance(policy, str):
+                        apply_correction(c, os_, i, s_eff * policy, cfg.clip * s_eff)
+                    if count % keep == 0 and slot < nbuf:
+                        xb[slot].copy_(xs[i])
+                        tb[slot].copy_(ts[i])
+                        slot += 1
+                    count += 1
+            stream.synchronize()
+            fine_b.close()
+            cur_b.close()
+            return slot
+
+        def train(filled, iters, lr0):
+            for it in range(iters):
+                idx = torch.from_numpy(rng.choice(filled, size=min(cfg.batch, filled),
+                                                  replace=False)).to(dev)
+                lr = lr0 * (0.1 if it >= 0.8 * iters else 0.3 if it >= 0.5 * iters else 1.0)
+                losses.append(net.train_step(xb[idx].contiguous(), tb[idx].contiguous(), lr))
+                if it % 500 == 0:
+                    say(f"iteration {it}/{iters} loss {losses[-1]:.4e}")
+            net.synchronize()
+
         t0 = time.perf_counter()
-        for m, c in zip(fine_b.members, cur_b.members):
-            restrict(m, c, fac)
-        cur_b.step(cfg.k)
-        fine_b.step(cfg.k * fac)
-        for i, (m, c, r) in enumerate(zip(fine_b.members, cur_b.members, refs)):
-            restrict(m, r, fac)
-            features(c, xb, slot, cfg.s_rho, cfg.s_u)
-            target(r, c, tb, slot, cfg.s_out)
-            slot = (slot + 1) % cfg.buffer
-            filled = min(filled + 1, cfg.buffer)
-        fine_b.step(spacing - cfg.k * fac)
-        cur_b.synchronize()
+        filled = generate(cfg.s_out, cfg.data_policy)
+        # targets to unit RMS; the applied correction is net output * s_eff
+        rms = float(torch.sqrt(torch.mean(tb[:filled] ** 2)))
+        rms = rms if rms > 0 else 1.0
+        tb[:filled] /= rms
+        s_eff = cfg.s_out * rms
         t_gen += time.perf_counter() - t0
         t0 = time.perf_counter()
-        for _ in range(cfg.iters_per_round):
-            idx = torch.from_numpy(rng.choice(filled, size=min(cfg.batch, filled), replace=False)).to(dev)
-            losses.append(net.train_step(xb[idx].contiguous(), tb[idx].contiguous(), cfg.lr))
+        train(filled, cfg.final_iters, cfg.lr)
         t_train += time.perf_counter() - t0
-        if rd % 50 == 0:
-            say(f"round {rd}/{rounds} loss {losses[-1]:.4e}")
-    t0 = time.perf_counter()
-    for it in range(cfg.final_iters):
-        idx = torch.from_numpy(rng.choice(filled, size=min(cfg.batch, filled), replace=False)).to(dev)
-        lr = cfg.lr * (0.5 if it > cfg.final_iters // 2 else 1.0)
-        losses.append(net.train_step(xb[idx].contiguous(), tb[idx].contiguous(), lr))
-    net.synchronize()
-    t_train += time.perf_counter() - t0
-    fine_b.close()
-    cur_b.close()
+        passes.append({"policy": cfg.data_policy, "final_loss": float(np.mean(losses[-20:]))})
+        for p in range(cfg.onpolicy_passes):
+            t0 = time.perf_counter()
+            filled = generate(s_eff, cfg.gain)
+            t_gen += time.perf_counter() - t0
+            t0 = time.perf_counter()
+            train(filled, cfg.onpolicy_iters, cfg.lr * 0.3)
+            t_train += time.perf_counter() - t0
+            passes.append({"policy": f"network, gain {cfg.gain}",
+                           "first_loss": losses[-cfg.onpolicy_iters],
+                           "final_loss": float(np.mean(losses[-20:]))})
+        del xb, tb, xs, ts, os_
     for r in refs:
         r.close()
-    del xb, tb
-    res["training"] = {"pairs": rounds * cfg.train_lattices, "iterations": len(losses),
-                       "first_loss": losses[0], "final_loss": float(np.mean(losses[-20:])),
-                       "data_seconds": round(t_gen, 2), "train_seconds": round(t_train, 2),
-                       "fine_steps_between_pairs": spacing}
+    info = {"pairs_per_pass": filled, "iterations": len(losses), "passes": passes,
+            "first_loss": losses[0], "final_loss": float(np.mean(losses[-20:])),
+            "loss_unit": "mean squared error / target variance",
+            "data_seconds": round(t_gen, 2), "train_seconds": round(t_train, 2),
+            "fine_steps_covered": rounds * cfg.k * fac}
+    return net, s_eff, info
 
-    # ---- judge on a held-out geometry ---------------------------------------
-    es = channel_spec(nf, tau=cfg.tau_fine, n_obstacles=cfg.n_obstacles, r_lo=cfg.r_lo,
-                      r_hi=cfg.r_hi, force=cfg.force_fine, seed=cfg.eval_seed)
-    cm = coarse_geometry(es.solid, fac)
-    fluid_c = cm == 0
-    stream = torch.cuda.Stream()
 
-    def coarse_lattice():
-        lat = lbm.Lattice(nc, nc, cfg.tau_coarse, lbm.F32, flags)
-        lat.set_force(force_c, 0.0)
-        lat.set_geometry(cm)
+def evaluate_correction(cfg: CorrectionConfig, net, s_eff: float, stream, gains=(1.0,),
+                        log=None, trace_every: int = 0) -> dict:
+    """Fine, coarse-only and coarse-plus-correction runs (one per gain) of a
+    held-out geometry, side by side on one stream; velocity L2 errors of the
+    coarse runs against the block-averaged fine run at each checkpoint, the
+    time of each run (CUDA events), and the first checkpoint at which a
+    corrected run failed its health check (mass drift or instability) — the
+    point where a production run would fall back to the fine grid."""
+    import torch
+    from . import lbm
+    say = log or (lambda *a: None)
+    nf, nc, fac = cfg.fine, cfg.coarse, cfg.factor
+    dev = torch.device("cuda")
+    (es,), (cs,) = _coarse_specs(cfg, [cfg.eval_seed])
+    fluid_c = cs.solid == 0
+    flags = es.flags | lbm.FAST
+
+    def lattice(n, tau, force, solid):
+        lat = lbm.Lattice(n, n, tau, lbm.F32, flags)
+        lat.set_force(*force)
+        lat.set_geometry(solid)
+        lat.set_stream(stream.cuda_stream)
         return lat
 
-    fine = lbm.Lattice(nf, nf, cfg.tau_fine, lbm.F32, flags)
-    fine.set_force(cfg.force_fine, 0.0)
-    fine.set_geometry(es.solid)
-    base, corr = coarse_lattice(), coarse_lattice()
-    restrict(fine, base, fac)
-    restrict(fine, corr, fac)
-    for lat in (fine, base, corr):
-        lat.set_stream(stream.cuda_stream)
+    fine = lattice(nf, cfg.tau_fine, es.force, es.solid)
+    base = lattice(nc, cfg.tau_coarse, cs.force, cs.solid)
+    corrs = [lattice(nc, cfg.tau_coarse, cs.force, cs.solid) for _ in gains]
+    for lat in [base] + corrs:
+        restrict(fine, lat, fac)
     chunk_f = cfg.horizon_fine // cfg.checkpoints
     chunk_c = chunk_f // fac
-    x1 = torch.zeros((1, 4, nc, nc), device=dev)
-    o1 = torch.zeros((1, 9, nc, nc), device=dev)
+    with torch.cuda.stream(stream):
+        x1 = torch.zeros((1, 4, nc, nc), device=dev)
+        o1 = torch.zeros((1, 9, nc, nc), device=dev)
+    stream.synchronize()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    t_fine = t_base = t_corr = 0.0
-    err_base, err_corr = [], []
-    fallback_at = None
-    mass0 = corr.health()["mass"]
+
+    def timed(fn):
+        ev0.record(stream)
+        fn()
+        ev1.record(stream)
+        ev1.synchronize()
+        return ev0.elapsed_time(ev1) / 1e3
+
+    t_fine = t_base = 0.0
+    t_corr = [0.0] * len(gains)
+    err_base, err_corr = [], [[] for _ in gains]
+    fallback_at = [None] * len(gains)
+    mass0 = [c.health()["mass"] for c in corrs]
+    trace = []
+    ncorr = 0
     for cp in range(cfg.checkpoints):
-        ev0.record(stream)
-        fine.step(chunk_f)
-        ev1.record(stream)
-        ev1.synchronize()
-        t_fine += ev0.elapsed_time(ev1) / 1e3
-        ev0.record(stream)
-        base.step(chunk_c)
-        ev1.record(stream)
-        ev1.synchronize()
-        t_base += ev0.elapsed_time(ev1) / 1e3
-        ev0.record(stream)
-        done = 0
-        while done < chunk_c:
-            n = min(cfg.k, chunk_c - done)
-            corr.step(n)
-            done += n
-            if n == cfg.k:
-                features(corr, x1, 0, cfg.s_rho, cfg.s_u)
-                net.forward(x1, o1)
-                apply_correction(corr, o1, 0, cfg.s_out)
-        ev1.record(stream)
-        ev1.synchronize()
-        t_corr += ev0.elapsed_time(ev1) / 1e3
-        # periodic check of the corrected run (the fine grid is the fallback)
-        h = corr.health()
-        if fallback_at is None and (h["unstable"] or abs(h["mass"] - mass0) > cfg.mass_tolerance * mass0):
-            fallback_at = (cp + 1) * chunk_f
+        t_fine += timed(lambda: fine.step(chunk_f))
+        t_base += timed(lambda: base.step(chunk_c))
+        for g, (gain, corr) in enumerate(zip(gains, corrs)):
+            def run():
+                nonlocal ncorr
+                done = 0
+                while done < chunk_c:
+                    n = min(cfg.k, chunk_c - done)
+                    corr.step(n)
+                    done += n
+                    if n == cfg.k:
+                        features(corr, x1, 0, cfg.s_rho, cfg.s_u)
+                        net.forward(x1, o1)
+                        apply_correction(corr, o1, 0, s_eff * gain, cfg.clip * s_eff)
+                        if trace_every and g == 0:
+                            ncorr += 1
+                            if ncorr % trace_every == 0:
+                                trace.append({"correction": ncorr,
+                                              "out_abs_max": float(o1.abs().max()),
+                                              "out_rms": float(o1.pow(2).mean().sqrt()),
+                                              "in_abs_max": float(x1[:, :3].abs().max())})
+            t_corr[g] += timed(run)
+            h = corr.health()
+            if fallback_at[g] is None and (h["unstable"] or
+                                           abs(h["mass"] - mass0[g]) > cfg.mass_tolerance * mass0[g]):
+                fallback_at[g] = (cp + 1) * chunk_f
         rho, ux, uy = fine.moments()
         rx, ry = _block_velocity(rho, ux, uy, es.solid, fac)
         _, bx, by = base.moments()
-        _, cx, cy = corr.moments()
         err_base.append(_l2(bx, by, rx, ry, fluid_c))
-        err_corr.append(_l2(cx, cy, rx, ry, fluid_c))
-        say(f"checkpoint {cp + 1}: coarse {err_base[-1]:.4f} corrected {err_corr[-1]:.4f}")
+        for g, corr in enumerate(corrs):
+            _, cx, cy = corr.moments()
+            err_corr[g].append(_l2(cx, cy, rx, ry, fluid_c))
+        say(f"checkpoint {cp + 1}: coarse {err_base[-1]:.4f} corrected "
+            + " ".join(f"{e[-1]:.4f}" for e in err_corr))
     u_rms = float(np.sqrt(np.mean((rx ** 2 + ry ** 2)[fluid_c])))
-    for lat in (fine, base, corr):
+    for lat in [fine, base] + corrs:
         lat.close()
-    net.close()
-    res["evaluation"] = {
-        "fine_equivalent_steps": cfg.horizon_fine, "checkpoints": cfg.checkpoints,
-        "u_l2_coarse_only": err_base, "u_l2_corrected": err_corr,
-        "u_l2_coarse_only_mean": float(np.mean(err_base)),
-        "u_l2_corrected_mean": float(np.mean(err_corr)),
-        "u_l2_coarse_only_final": err_base[-1], "u_l2_corrected_final": err_corr[-1],
-        "u_rms_fine_final": u_rms,
-        "fine_seconds": round(t_fine, 4), "coarse_seconds": round(t_base, 4),
-        "corrected_seconds": round(t_corr, 4),
-        "time_to_solution_ratio": round(t_fine / max(t_corr, 1e-12), 2),
-        "fallback_triggered_at_fine_step": fallback_at,
-    }
+    out = {"fine_equivalent_steps": cfg.horizon_fine, "checkpoints": cfg.checkpoints,
+           "u_l2_coarse_only": err_base, "u_l2_coarse_only_mean": float(np.mean(err_base)),
+           "u_l2_coarse_only_final": err_base[-1], "u_rms_fine_final": u_rms,
+           "fine_seconds": round(t_fine, 4), "coarse_seconds": round(t_base, 4), "corrected": []}
+    for g, gain in enumerate(gains):
+        out["corrected"].append({
+            "gain": gain, "u_l2": err_corr[g], "u_l2_mean": float(np.mean(err_corr[g])),
+            "u_l2_final": err_corr[g][-1], "seconds": round(t_corr[g], 4),
+            "time_to_solution_ratio": round(t_fine / max(t_corr[g], 1e-12), 2),
+            "fallback_triggered_at_fine_step": fallback_at[g]})
+    if trace:
+        out["trace"] = trace
+    return out
+
+
+def run_correction_experiment(cfg: CorrectionConfig, log=None, gains=None, trace_every=0) -> dict:
+    """Trains the correction (train_correction) and judges it on a held-out
+    geometry (evaluate_correction).  Returns a result dict."""
+    import torch
+    stream = torch.cuda.Stream()
+    res = {"config": {k: v for k, v in cfg.__dict__.items() if k != "extra"},
+           "tau_coarse": cfg.tau_coarse, "force_coarse": cfg.force_fine * cfg.factor}
+    net, s_eff, res["training"] = train_correction(cfg, stream, log)
+    res["training"]["target_rms"] = s_eff
+    try:
+        res["evaluation"] = evaluate_correction(cfg, net, s_eff, stream,
+                                                gains=gains or (cfg.gain,), log=log,
+                                                trace_every=trace_every)
+    finally:
+        net.close()
     return res

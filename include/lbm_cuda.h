@@ -238,6 +238,22 @@ int lbm_batch_set_stream(lbm_batch* batch, void* stream);
  * mode is reused without timing.  steps_per_trial <= 0 selects 24.         */
 int lbm_batch_autotune(lbm_batch* batch, const char* cache_path, int steps_per_trial);
 
+/* ---- colour map (src/render.rs) ------------------------------------------
+ * Renders the lattice's moments into an RGBA8 image of w x h pixels, pixel
+ * (x, y) at byte (y * w + x) * 4, alpha 255, the way render_scalar_field /
+ * render_vector_field (src/render.rs:23-207) colour a field: value =
+ * logistic(z-score over all cells), hue 0 and saturation 1 for the scalar
+ * modes, hue = (atan2(vy, vx) + pi) / 2pi and saturation 0.8 for the vector
+ * modes (z-score of vx^2 + vy^2), HSV -> RGB, channel = clamp(round(256 c)).
+ * With geometry_overlay, solid cells are (0, 0, 255) as in render_geometry
+ * (src/render.rs:7-21).  Momentum density is rho * u of the moments.
+ * rgba is a device pointer when on_device, else host memory.               */
+#define LBM_RENDER_DENSITY 0
+#define LBM_RENDER_SPEED 1
+#define LBM_RENDER_VELOCITY 2
+#define LBM_RENDER_MOMENTUM 3
+int lbm_render(lbm_lattice* lat, int mode, int geometry_overlay, uint8_t* rgba, int on_device);
+
 /* ---- learned coarse-grid correction --------------------------------------
  * No reference counterpart.  A 4-layer 3x3 convolutional network (channels
  * 4 -> 32 -> 32 -> 32 -> 9, GELU, bf16 weights, f32 accumulation on the
@@ -265,6 +281,10 @@ int lbm_cnn_gradients(lbm_cnn* net, const float* in, const float* target, int ba
 /* One Adam step (beta1 0.9, beta2 0.999) on the MSE loss.                  */
 int lbm_cnn_train_step(lbm_cnn* net, const float* in, const float* target, int batch,
                        float lr, float* loss);
+/* Issue the net's work on `stream` (a cudaStream_t; NULL = the net's own
+ * stream).  Calls read their input tensors in that stream's order, so a
+ * caller that fills them on another stream orders the two itself.          */
+int lbm_cnn_set_stream(lbm_cnn* net, void* stream);
 int lbm_cnn_synchronize(lbm_cnn* net);
 
 /* Fine -> coarse lattice (both f32; coarse sides = fine sides / factor):
@@ -273,13 +293,15 @@ int lbm_restrict(lbm_lattice* fine, lbm_lattice* coarse, int factor);
 /* The network input of a lattice as image `image` of a device tensor
  * (batch, 4, h, w) f32.                                                     */
 int lbm_coarse_features(lbm_lattice* lat, float s_rho, float s_u, int image, float* in);
-/* f_i += d_i - w_i * sum_j d_j with d_i = scale * corr[image][i], on the
- * fluid cells of an f32 lattice (the correction never changes a cell's mass). */
-int lbm_coarse_apply(lbm_lattice* lat, const float* corr, int image, float scale);
-/* target[image][i] = (f_i(ref) - f_eq_i(rho, j/rho of cur)) / scale for two
- * f32 lattices (ref holding equilibria, as lbm_restrict writes them): the
- * population change that moves cur's density and momentum onto ref's and
- * leaves cur's non-equilibrium part alone.                                  */
+/* f_i += d_i - w_i * sum_j d_j with d_i = scale * corr[image][i] (each
+ * clamped to +-max_abs when max_abs > 0) on the fluid cells of an f32
+ * lattice: the correction never changes a cell's mass.                     */
+int lbm_coarse_apply(lbm_lattice* lat, const float* corr, int image, float scale, float max_abs);
+/* target[image][i] = (f_eq_i(rho_cur, u_ref) - f_eq_i(rho_cur, u_cur)) / scale
+ * with u = j / rho of the stored states, zero on cur's solid cells, for two
+ * f32 lattices of one size (ref holding equilibria, as lbm_restrict writes
+ * them): the population change that moves cur's velocity onto ref's and
+ * leaves its density and non-equilibrium part alone.                        */
 int lbm_coarse_target(lbm_lattice* ref, lbm_lattice* cur, float scale, int image, float* target);
 
 #ifdef __cplusplus

@@ -124,10 +124,10 @@ def test_features_apply_target(gpu):
         uy = (0.01 * rng.normal(size=(32, 128))).astype(np.float32)
         a.init_equilibrium(rho, ux, uy)
         b.init_equilibrium(np.ones_like(rho), ux * 0, uy * 0)
+        solid = spec.solid.astype(bool)
         x = torch.zeros((2, 4, 32, 128), device="cuda")
         features(a, x, 1, 100.0, 50.0)
         r, vx, vy = a.moments()
-        solid = spec.solid.astype(bool)
         xs = x[1].cpu().numpy()
         np.testing.assert_allclose(xs[0], np.where(solid, 0, (r - 1) * 100), rtol=1e-6, atol=1e-6)
         np.testing.assert_allclose(xs[1], np.where(solid, 0, vx * 50), rtol=1e-6, atol=1e-7)
@@ -135,14 +135,29 @@ def test_features_apply_target(gpu):
         assert float(x[0].abs().sum()) == 0.0
         t = torch.zeros((1, 9, 32, 128), device="cuda")
         target(a, b, t, 0, 1e-3)
-        fa, fb = a.get_populations(), b.get_populations()
-        # b holds equilibria, so f_eq of its own moments is fb itself
-        np.testing.assert_allclose(t[0].cpu().numpy(), (fa - fb) / 1e-3, rtol=1e-5, atol=1e-3)
+        fa, fb = a.get_populations().astype(np.float64), b.get_populations().astype(np.float64)
+        cx = np.array([0, 1, 0, -1, 0, 1, -1, -1, 1])[:, None, None]
+        cy = np.array([0, 0, 1, 0, -1, 1, 1, -1, -1])[:, None, None]
+        ra = fa.sum(axis=0)
+        uxa, uya = (fa * cx).sum(axis=0) / ra, (fa * cy).sum(axis=0) / ra
+        tg = t[0].cpu().numpy().astype(np.float64)
+        rb = fb.sum(axis=0)
+        # b is at rest: the target is f_eq(rho_b, u(a)) - f_eq(rho_b, 0), over the scale
+        shift = (oracle.equilibrium(rb.astype(np.float32), uxa.astype(np.float32), uya.astype(np.float32))
+                 .astype(np.float64) - oracle.equilibrium(rb.astype(np.float32), 0 * rho, 0 * rho))
+        np.testing.assert_allclose(tg, np.where(solid[None], 0, shift / 1e-3), rtol=0, atol=2e-4)
         apply_correction(b, t, 0, 1e-3)
-        got = b.get_populations()
+        got = b.get_populations().astype(np.float64)
         w = np.array([16, 4, 4, 4, 4, 1, 1, 1, 1], np.float64)[:, None, None] / 36
-        d = (fa - fb).astype(np.float64)
-        exp = np.where(solid[None], fb, fb + d - w * d.sum(axis=0, keepdims=True))
-        np.testing.assert_allclose(got, exp, rtol=0, atol=3e-7)
+        d = tg * 1e-3
+        np.testing.assert_allclose(got, np.where(solid[None], fb, fb + d - w * d.sum(axis=0)),
+                                   rtol=0, atol=3e-7)
         # mass per fluid cell unchanged by the correction
         np.testing.assert_allclose(got.sum(axis=0), fb.sum(axis=0), rtol=0, atol=1e-6)
+        # clamped correction: each population change limited to +-max_abs first
+        b.init_equilibrium(np.ones_like(rho), ux * 0, uy * 0)
+        apply_correction(b, t, 0, 1e-3, max_abs=2e-4)
+        got = b.get_populations().astype(np.float64)
+        dc = np.clip(d, -2e-4, 2e-4)
+        np.testing.assert_allclose(got, np.where(solid[None], fb, fb + dc - w * dc.sum(axis=0)),
+                                   rtol=0, atol=3e-7)
