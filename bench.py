@@ -22,6 +22,13 @@ populations per step) are larger than L2, so no L2 flush is needed.
   roofline  algorithmic bytes (9 loads + 9 stores of 4 B + 1 B solid mask =
           73 B per cell) / average step time against the measured HBM copy
           bandwidth.
+  batch   512 uneven lattices (sides U[64, 1024]) stepped together, autotuned.
+  large   16384^2 with 16-bit deviation storage against 8192^2 f32, and their
+          rho/u L2 errors against f64 on a 1024^2 window.
+  learned the coarse-grid correction: 2048^2 fine vs 512^2 coarse channel,
+          training on the GPU, velocity L2 of coarse-only and corrected runs
+          against the fine run, time-to-solution ratio, and the network's
+          forward throughput on the tensor cores.
 
 --impl reference times the CPU implementation of the same step, restated op
 by op the way lbm.rs drives ArrayFire (oracle/, the reference cannot be built
@@ -66,6 +73,9 @@ def parse_args():
     p.add_argument("--no-large", action="store_true",
                    help="skip the 16384^2 f16 / 8192^2 f32 comparison")
     p.add_argument("--large-steps", type=int, default=500)
+    p.add_argument("--no-learned", action="store_true",
+                   help="skip the learned coarse-grid correction (train + judge)")
+    p.add_argument("--learned-iters", type=int, default=3000, help="Adam iterations")
     return p.parse_args()
 
 
@@ -336,6 +346,7 @@ def run_ours(args):
     e2e = run_e2e(spec, args, torch, dist)
     batch = None if args.no_batch or world > 1 else run_batch(args, torch)
     large = None if args.no_large or world > 1 else run_large(args, torch)
+    learned = None if args.no_learned or world > 1 else run_learned(args, torch)
 
     peak, peak_kind = measured_peak_gbs()
     bpc = BYTES_F32 + BYTES_MASK
@@ -382,6 +393,7 @@ def run_ours(args):
             "cpu_baseline": cpu,
             "batch": batch,
             "large": large,
+            "learned": learned,
         }
         print(json.dumps(line), flush=True)
     if dist is not None:
@@ -431,6 +443,42 @@ def run_batch(args, torch):
             "tiles_cells_per_thread_by_width_class": tiles,
             "launches_per_step": "one per non-empty (tile width, path) list",
             "stable": all(not h["unstable"] for h in health)}
+
+
+def run_learned(args, torch):
+    """The learned coarse-grid correction: 2048^2 fine channel (tau 0.55, 64
+    obstacles) against the 512^2 coarse lattice of equal viscosity (tau_c =
+    0.5125, F_c = 4 F), snapshot pairs from the batched fine LBM, training on
+    the GPU, then the held-out geometry over 20000 fine-equivalent steps:
+    velocity L2 of coarse-only and corrected runs against the fine run and the
+    time-to-solution ratio.  Also the correction network's forward throughput
+    (tcgen05 implicit-GEMM convolutions) on 8 coarse images."""
+    from chemsim_gb300.learned import (CorrectionConfig, evaluate_correction, forward_throughput,
+                                       train_correction)
+    cfg = CorrectionConfig(final_iters=args.learned_iters)
+    stream = torch.cuda.Stream()
+    t0 = time.perf_counter()
+    net, s_eff, info = train_correction(cfg, stream)
+    try:
+        ev = evaluate_correction(cfg, net, s_eff, stream, gains=(cfg.gain,))
+    finally:
+        net.close()
+    wall = time.perf_counter() - t0
+    fwd = forward_throughput(8, cfg.coarse)
+    corr = ev["corrected"][0]
+    return {"workload": f"fine {cfg.fine}^2 tau {cfg.tau_fine} vs coarse {cfg.coarse}^2 tau "
+                        f"{cfg.tau_coarse:.4f}, {cfg.n_obstacles} obstacles, correction every "
+                        f"{cfg.k} coarse steps, {cfg.horizon_fine} fine-equivalent steps",
+            "training": info, "u_l2_coarse_only_mean": round(ev["u_l2_coarse_only_mean"], 5),
+            "u_l2_coarse_only_final": round(ev["u_l2_coarse_only_final"], 5),
+            "u_l2_corrected_mean": round(corr["u_l2_mean"], 5),
+            "u_l2_corrected_final": round(corr["u_l2_final"], 5), "gain": corr["gain"],
+            "fine_seconds": ev["fine_seconds"], "coarse_only_seconds": ev["coarse_seconds"],
+            "corrected_seconds": corr["seconds"],
+            "time_to_solution_ratio": corr["time_to_solution_ratio"],
+            "fallback_triggered_at_fine_step": corr["fallback_triggered_at_fine_step"],
+            "wall_seconds": round(wall, 1),
+            "forward": fwd}
 
 
 def run_large(args, torch):

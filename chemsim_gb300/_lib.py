@@ -114,6 +114,8 @@ SIGNATURES = {
     "lbm_batch_set_stream": (_i32, [_vp, _vp]),
     "lbm_batch_autotune": (_i32, [_vp, ctypes.c_char_p, _i32]),
     "lbm_render": (_i32, [_vp, _i32, _i32, _vp, _i32]),
+    "lbm_save": (_i32, [_vp, ctypes.c_char_p]),
+    "lbm_load": (_i32, [_vp, ctypes.c_char_p]),
     "lbm_cnn_create": (_i32, [_i32, _i32, _i32, ctypes.c_uint64, ctypes.POINTER(_vp)]),
     "lbm_cnn_destroy": (_i32, [_vp]),
     "lbm_cnn_param_count": (_i32, [_vp, ctypes.POINTER(_i64)]),
@@ -123,6 +125,10 @@ SIGNATURES = {
     "lbm_cnn_gradients": (_i32, [_vp, _vp, _vp, _i32, ctypes.POINTER(_f32), _vp]),
     "lbm_cnn_train_step": (_i32, [_vp, _vp, _vp, _i32, _f32, ctypes.POINTER(_f32)]),
     "lbm_cnn_set_stream": (_i32, [_vp, _vp]),
+    "lbm_cnn_save": (_i32, [_vp, ctypes.c_char_p]),
+    "lbm_cnn_load": (_i32, [_vp, ctypes.c_char_p]),
+    "lbm_coarse_run": (_i32, [_vp, _vp, _i32, _i32, _f32, _f32, _f32, _f32, _i32, _f32,
+                              ctypes.POINTER(_i64)]),
     "lbm_cnn_synchronize": (_i32, [_vp]),
     "lbm_restrict": (_i32, [_vp, _vp, _i32]),
     "lbm_coarse_features": (_i32, [_vp, _f32, _f32, _i32, _vp]),

@@ -6,6 +6,7 @@
 // State::step's three phases (:694-714) are one fused kernel launch per step;
 // runs of steps replay a captured CUDA graph.
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <string>
 #include <type_traits>
@@ -743,6 +744,93 @@ int lbm_set_tile(lbm_lattice* L, int cells_per_thread, int rows_per_block) {
     L->vcells = v; L->rows = r; L->dirty = true; ++L->version;
     if (int rc = refresh_tiles(L)) return rc;
     LBM_CUDA(cudaStreamSynchronize(L->stream));
+    return LBM_OK;
+}
+
+// ---- checkpoint file ------------------------------------------------------
+// Header (little-endian, 96 bytes) then the nine population planes in the
+// lattice's storage type, row-major y * w + x (the C-ABI population layout;
+// 16-bit storage keeps its raw deviation values, so a round trip is exact),
+// then the solid mask (w * h bytes) when the lattice has one.
+struct CheckpointHeader {
+    char magic[8];            // "LBMSTATE"
+    int32_t version;          // 1
+    int32_t w, h, precision, flags, collision, has_solid, reserved0;
+    float tau, tau_minus, dx, dt, fx, fy, time, reserved1;
+    int64_t steps;
+    int64_t reserved2[2];
+};
+static_assert(sizeof(CheckpointHeader) == 96, "checkpoint header layout");
+constexpr char kStateMagic[8] = {'L', 'B', 'M', 'S', 'T', 'A', 'T', 'E'};
+
+int lbm_save(lbm_lattice* L, const char* path) {
+    if (int rc = check_handle(L)) return rc;
+    if (!path) return fail(LBM_ERR_INVALID_ARGUMENT, "null path");
+    DeviceGuard g(L->dev);
+    CheckpointHeader hd{};
+    std::memcpy(hd.magic, kStateMagic, 8);
+    hd.version = 1;
+    hd.w = L->w; hd.h = L->h; hd.precision = L->precision; hd.flags = L->flags;
+    hd.collision = L->collision; hd.has_solid = L->has_solid ? 1 : 0;
+    hd.tau = L->tau; hd.tau_minus = L->tau_minus; hd.dx = L->dx; hd.dt = L->dt;
+    hd.fx = L->fx; hd.fy = L->fy; hd.time = L->time; hd.steps = L->steps;
+    const size_t row = size_t(L->w) * L->esize, n = size_t(L->h) * row;
+    std::vector<uint8_t> host(9 * n + (L->has_solid ? size_t(L->w) * L->h : 0));
+    for (int i = 0; i < 9; ++i)
+        LBM_CUDA(cudaMemcpy2DAsync(host.data() + i * n, row,
+                                   static_cast<uint8_t*>(L->buf[L->cur]) + size_t(i) * L->plane * L->esize,
+                                   size_t(L->pitch) * L->esize, row, L->h, cudaMemcpyDeviceToHost,
+                                   L->stream));
+    if (L->has_solid)
+        LBM_CUDA(cudaMemcpy2DAsync(host.data() + 9 * n, L->w, L->solid, L->mpitch, L->w, L->h,
+                                   cudaMemcpyDeviceToHost, L->stream));
+    LBM_CUDA(cudaStreamSynchronize(L->stream));
+    FILE* fp = std::fopen(path, "wb");
+    if (!fp) return fail(LBM_ERR_INVALID_ARGUMENT, std::string("cannot open ") + path);
+    const bool ok = std::fwrite(&hd, sizeof(hd), 1, fp) == 1 &&
+                    std::fwrite(host.data(), 1, host.size(), fp) == host.size();
+    if (std::fclose(fp) != 0 || !ok) return fail(LBM_ERR_INVALID_ARGUMENT, "checkpoint write failed");
+    return LBM_OK;
+}
+
+int lbm_load(lbm_lattice* L, const char* path) {
+    if (int rc = check_handle(L)) return rc;
+    if (!path) return fail(LBM_ERR_INVALID_ARGUMENT, "null path");
+    FILE* fp = std::fopen(path, "rb");
+    if (!fp) return fail(LBM_ERR_INVALID_ARGUMENT, std::string("cannot open ") + path);
+    CheckpointHeader hd{};
+    bool ok = std::fread(&hd, sizeof(hd), 1, fp) == 1 && std::memcmp(hd.magic, kStateMagic, 8) == 0 &&
+              hd.version == 1;
+    if (ok && (hd.w != L->w || hd.h != L->h || hd.precision != L->precision ||
+               (hd.flags & ~LBM_FAST) != (L->flags & ~LBM_FAST))) {
+        std::fclose(fp);
+        return fail(LBM_ERR_INVALID_ARGUMENT,
+                    "checkpoint size, precision or boundary flags differ from the lattice's");
+    }
+    const size_t row = size_t(L->w) * L->esize, n = size_t(L->h) * row;
+    std::vector<uint8_t> host;
+    if (ok) {
+        host.resize(9 * n + (hd.has_solid ? size_t(L->w) * L->h : 0));
+        ok = std::fread(host.data(), 1, host.size(), fp) == host.size();
+    }
+    std::fclose(fp);
+    if (!ok) return fail(LBM_ERR_INVALID_ARGUMENT, "not a lattice checkpoint (or truncated)");
+    DeviceGuard g(L->dev);
+    if (int rc = lbm_set_discretization(L, hd.dx, hd.dt)) return rc;
+    if (int rc = lbm_set_collision(L, hd.collision, hd.tau, hd.tau_minus)) return rc;
+    if (int rc = lbm_set_force(L, hd.fx, hd.fy)) return rc;
+    if (int rc = lbm_set_geometry(L, hd.has_solid ? host.data() + 9 * n : nullptr)) return rc;
+    for (int i = 0; i < 9; ++i)
+        LBM_CUDA(cudaMemcpy2DAsync(static_cast<uint8_t*>(L->buf[L->cur]) + size_t(i) * L->plane * L->esize,
+                                   size_t(L->pitch) * L->esize, host.data() + i * n, row, row, L->h,
+                                   cudaMemcpyHostToDevice, L->stream));
+    LBM_CUDA(cudaStreamSynchronize(L->stream));
+    L->flags = (L->flags & ~LBM_FAST) | (hd.flags & LBM_FAST);
+    L->time = hd.time;
+    L->steps = hd.steps;
+    L->mom_valid = false;
+    L->dirty = true;
+    ++L->version;
     return LBM_OK;
 }
 

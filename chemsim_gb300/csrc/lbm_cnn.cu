@@ -16,7 +16,9 @@
 // the 4 warps read their 32 lanes back with tcgen05.ld and run the epilogue
 // (bias, GELU, stores).  The same kernel computes input gradients with the
 // flipped, channel-transposed weights and a GELU' epilogue.
+#include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -34,6 +36,7 @@ constexpr int kCin[kLayers] = {4, 32, 32, 32};
 constexpr int kCout[kLayers] = {32, 32, 32, 9};
 constexpr int kTileM = 128;                       // pixels per CTA
 constexpr uint32_t kWaitPolls = 1u << 22;         // bounded mbarrier wait
+constexpr char kCnnMagic[8] = {'L', 'B', 'M', 'C', 'N', 'N', '0', '1'};
 
 __host__ __device__ constexpr int pad16(int c) { return (c + 15) / 16 * 16; }
 
@@ -59,12 +62,14 @@ struct ConvArgs {
     int* err;
 };
 
-// Dynamic shared memory of a conv CTA: A halo tile, B (weights), barrier.
-// The A region is sized for 3 rows x 4 blocks x 130 pixels plus room so
-// that every descriptor's reach stays inside the allocation.
-constexpr int kARegion = 65536;
+// Dynamic shared memory of a conv CTA: A halo tile (3 rows x CBI blocks x
+// 130 pixels x 16 B; the descriptors of the 9 taps reach exactly its last
+// byte), B (weights), two mbarriers and the TMEM address slot.
+constexpr int kRowBytes = (kTileM + 2) * 16;
+constexpr int kARegion = 3 * 4 * kRowBytes + 640;      // 25600, a multiple of 1024
 constexpr int kBRegion = 9 * 2 * 4 * 2 * 128;      // CBI/2 <= 2, NO/8 <= 4
 constexpr int kConvSmem = kARegion + kBRegion + 64;
+static_assert(kARegion % 1024 == 0 && kARegion >= 3 * 4 * kRowBytes, "A region");
 
 template <int CBI, int NO, int MODE>
 __global__ void __launch_bounds__(128)
@@ -72,42 +77,50 @@ conv3x3_tc_kernel(const ConvArgs a) {
     extern __shared__ __align__(1024) uint8_t smem[];
     uint8_t* sA = smem;
     uint8_t* sB = smem + kARegion;
-    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + kARegion + kBRegion);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + kARegion + kBRegion);   // MMAs done
+    uint64_t* lbar = bar + 1;                                                  // tiles staged
     uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + kARegion + kBRegion + 16);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int x0 = blockIdx.x * kTileM, y = blockIdx.y, b = blockIdx.z;
     const int H = a.H, W = a.W;
+    // B: 9 * CBI/2 K-steps of (NO/8 x 2) core matrices; A: rows y-1..y+1 of
+    // every input block, pixels x0-1 .. x0+128 (in the halo, so in bounds:
+    // W is a multiple of 128 and the layout has one halo pixel each side)
+    constexpr uint32_t kBBytes = 9 * (CBI / 2) * (NO / 8) * 2 * 128;
+    constexpr uint32_t kABytes = 3 * CBI * kRowBytes;
+    static_assert(kBBytes <= kBRegion && kABytes <= kARegion, "tiles fit");
 
-    if (tid == 0) lbmtc::mbar_init(bar, 1);
+    if (tid == 0) {
+        lbmtc::mbar_init(bar, 1);
+        lbmtc::mbar_init(lbar, 1);
+    }
     if (warp == 0) lbmtc::tmem_alloc(tslot, 32);
-
-    // stage B: 9 * CBI/2 steps of (NO/8 x 2) core matrices, a linear copy
-    constexpr int kBBytes = 9 * (CBI / 2) * (NO / 8) * 2 * 128;
-    {
-        const uint4* src = reinterpret_cast<const uint4*>(a.wpack);
-        uint4* dst = reinterpret_cast<uint4*>(sB);
-        for (int k = tid; k < kBBytes / 16; k += 128) dst[k] = src[k];
-    }
-    // stage A: rows y-1..y+1, all input blocks, pixels x0-1 .. x0+128
-    {
-        uint4* dst = reinterpret_cast<uint4*>(sA);
-        constexpr int kChunks = 3 * CBI * (kTileM + 2);
-        for (int k = tid; k < kChunks; k += 128) {
-            const int px = k % (kTileM + 2);
-            const int rc = k / (kTileM + 2);           // r * CBI + cb
-            const int cb = rc % CBI, r = rc / CBI;
-            const uint4* src = reinterpret_cast<const uint4*>(a.in) +
-                               cb8_chunk(b, y + r - 1, cb, x0 + px - 1, H, W, CBI);
-            dst[k] = __ldg(src);
-        }
-    }
-    lbmtc::fence_proxy_async_smem();
-    lbmtc::fence_before_sync();
     __syncthreads();
+    if (tid == 0) {
+        // stage both operands with the bulk-copy engine: one copy of the
+        // packed weights and one contiguous 2080-byte row segment per
+        // (row, input block)
+        lbmtc::mbar_expect_tx(lbar, kBBytes + kABytes);
+        lbmtc::bulk_g2s(sB, a.wpack, kBBytes, lbar);
+        const uint4* in = reinterpret_cast<const uint4*>(a.in);
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+            for (int cb = 0; cb < CBI; ++cb)
+                lbmtc::bulk_g2s(sA + (r * CBI + cb) * kRowBytes,
+                                in + cb8_chunk(b, y + r - 1, cb, x0 - 1, H, W, CBI), kRowBytes, lbar);
+    }
+    bool mine = lbmtc::mbar_wait_bounded(lbar, 0, kWaitPolls);
+    if (!mine) {
+        if (lane == 0) atomicExch(a.err, 1);
+        (void)lbmtc::mbar_wait_bounded(lbar, 0, kWaitPolls);   // let the copies land
+    }
+    lbmtc::fence_before_sync();                 // orders the TMEM allocation before the barrier
+    const bool staged = __syncthreads_and(mine);
     lbmtc::fence_after_sync();
     const uint32_t tmem = *tslot;
 
-    if (tid == 0) {
+    if (tid == 0 && staged) {
         constexpr uint32_t idesc = lbmtc::idesc_bf16_f32(kTileM, NO);
         const uint32_t a0 = lbmtc::smem_u32(sA), b0 = lbmtc::smem_u32(sB);
         uint32_t acc = 0;
@@ -128,8 +141,8 @@ conv3x3_tc_kernel(const ConvArgs a) {
         }
         lbmtc::mma_commit(bar);
     }
-    const bool done = lbmtc::mbar_wait_bounded(bar, 0, kWaitPolls);
-    if (!done) {
+    bool done = staged && lbmtc::mbar_wait_bounded(bar, 0, kWaitPolls);
+    if (staged && !done) {
         if (lane == 0) atomicExch(a.err, 1);
         (void)lbmtc::mbar_wait_bounded(bar, 0, kWaitPolls);   // let the MMAs drain
     }
@@ -386,6 +399,7 @@ struct lbm_cnn {
     __nv_bfloat16* z[kLayers] = {};    // pre-activations of layers 0..2 outputs (z[l] for layer l)
     __nv_bfloat16* gbuf[kLayers + 1] = {};  // gradients wrt layer outputs
     float* out = nullptr;              // NCHW f32, 9 channels
+    float* feat = nullptr;             // one image of features (4 x H x W f32), lbm_coarse_run
     float* dw_partial = nullptr;
     float* db_partial = nullptr;
     double* loss_partial = nullptr;
@@ -611,7 +625,7 @@ int lbm_cnn_destroy(lbm_cnn* N) {
     if (!N) return LBM_OK;
     if (N->stream) cudaStreamSynchronize(N->stream);
     void* ptrs[] = {N->params, N->grads, N->adam_m, N->adam_v, N->err, N->out, N->dw_partial,
-                    N->db_partial, N->loss_partial};
+                    N->db_partial, N->loss_partial, N->feat};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     for (int l = 0; l < kLayers; ++l) {
@@ -699,6 +713,84 @@ int lbm_cnn_train_step(lbm_cnn* N, const float* in_dev, const float* target_dev,
     CNN_CUDA(cudaGetLastError());
     if (int rc = repack(N)) return rc;
     return LBM_OK;
+}
+
+int lbm_cnn_save(lbm_cnn* N, const char* path) {
+    if (!N || !path) return cfail(LBM_ERR_INVALID_ARGUMENT, "null argument");
+    std::vector<float> p(N->nparams);
+    if (int rc = lbm_cnn_get_params(N, p.data())) return rc;
+    FILE* fp = std::fopen(path, "wb");
+    if (!fp) return cfail(LBM_ERR_INVALID_ARGUMENT, std::string("cannot open ") + path);
+    const int64_t n = N->nparams;
+    const bool ok = std::fwrite(kCnnMagic, 1, 8, fp) == 8 && std::fwrite(&n, 8, 1, fp) == 1 &&
+                    std::fwrite(p.data(), 4, p.size(), fp) == p.size();
+    if (std::fclose(fp) != 0 || !ok) return cfail(LBM_ERR_INVALID_ARGUMENT, "write failed");
+    return LBM_OK;
+}
+
+int lbm_cnn_load(lbm_cnn* N, const char* path) {
+    if (!N || !path) return cfail(LBM_ERR_INVALID_ARGUMENT, "null argument");
+    FILE* fp = std::fopen(path, "rb");
+    if (!fp) return cfail(LBM_ERR_INVALID_ARGUMENT, std::string("cannot open ") + path);
+    char magic[8] = {};
+    int64_t n = 0;
+    std::vector<float> p(N->nparams);
+    const bool ok = std::fread(magic, 1, 8, fp) == 8 && std::memcmp(magic, kCnnMagic, 8) == 0 &&
+                    std::fread(&n, 8, 1, fp) == 1 && n == N->nparams &&
+                    std::fread(p.data(), 4, p.size(), fp) == p.size();
+    std::fclose(fp);
+    if (!ok) return cfail(LBM_ERR_INVALID_ARGUMENT, "not a weight file of this network");
+    return lbm_cnn_set_params(N, p.data());
+}
+
+int lbm_coarse_run(lbm_lattice* lat, lbm_cnn* N, int nsteps, int k, float s_rho, float s_u,
+                   float scale, float max_abs, int check_every, float mass_tolerance,
+                   int64_t* fallback_step) {
+    if (!lat || !N || !fallback_step) return cfail(LBM_ERR_INVALID_ARGUMENT, "null argument");
+    *fallback_step = -1;
+    if (nsteps < 0 || k < 1 || check_every < 0 || !(mass_tolerance > 0.f))
+        return cfail(LBM_ERR_INVALID_ARGUMENT, "need nsteps >= 0, k >= 1, check_every >= 0, "
+                                               "mass_tolerance > 0");
+    if (lat->precision != LBM_F32 || lat->w != N->W || lat->h != N->H)
+        return cfail(LBM_ERR_INVALID_ARGUMENT, "need an f32 lattice of the network's size");
+    if (!N->feat) {
+        CNN_CUDA(cudaMalloc(&N->feat, size_t(4) * N->H * N->W * 4));
+        CNN_CUDA(cudaMemsetAsync(N->feat, 0, size_t(4) * N->H * N->W * 4, N->stream));
+    }
+    CNN_CUDA(cudaStreamSynchronize(N->stream));
+    const cudaStream_t saved = N->stream;
+    N->stream = lat->stream;                       // one stream orders step, net and apply
+    auto finish = [&](int rc) {
+        N->stream = saved;
+        return rc;
+    };
+    lbm_health h0{};
+    if (int rc = lbm_check(lat, &h0)) return finish(rc);
+    int done = 0, corrections = 0;
+    while (done < nsteps) {
+        const int n = std::min(k, nsteps - done);
+        if (int rc = lbm_step(lat, n)) return finish(rc);
+        done += n;
+        if (n < k) break;
+        if (int rc = lbm_coarse_features(lat, s_rho, s_u, 0, N->feat)) return finish(rc);
+        nchw_to_cb8_kernel<<<grid_of(int64_t(N->H) * N->W * 2, 256), 256, 0, N->stream>>>(
+            N->feat, 1, 4, N->H, N->W, 2, N->x[0]);
+        if (cudaGetLastError() != cudaSuccess) return finish(cfail(LBM_ERR_CUDA, "features launch"));
+        if (int rc = forward_impl(N, 1)) return finish(rc);
+        if (int rc = lbm_coarse_apply(lat, N->out, 0, scale, max_abs)) return finish(rc);
+        ++corrections;
+        if (check_every > 0 && corrections % check_every == 0) {
+            // the periodic check: an unstable state or a mass drift past the
+            // tolerance ends the coarse run; the caller continues on the fine grid
+            lbm_health h{};
+            if (int rc = lbm_check(lat, &h)) return finish(rc);
+            if (h.unstable || std::fabs(h.mass - h0.mass) > double(mass_tolerance) * std::fabs(h0.mass)) {
+                *fallback_step = lat->steps;
+                break;
+            }
+        }
+    }
+    return finish(check_err(N));
 }
 
 int lbm_cnn_set_stream(lbm_cnn* N, void* stream) {

@@ -191,6 +191,9 @@ struct StepArgs {
 
 // Strict arithmetic: one IEEE rounding per operation, no contraction; the
 // operation order of src/lbm.rs.  Fast arithmetic: contracted / simplified.
+#ifndef LBM_RCP_APPROX
+#define LBM_RCP_APPROX 0
+#endif
 template <bool FAST> struct Ar;
 template <> struct Ar<false> {
     __device__ static float add(float a, float b) { return __fadd_rn(a, b); }
@@ -206,7 +209,17 @@ template <> struct Ar<true> {
     __device__ static float add(float a, float b) { return a + b; }
     __device__ static float sub(float a, float b) { return a - b; }
     __device__ static float mul(float a, float b) { return a * b; }
+#if LBM_RCP_APPROX
+    // one MUFU reciprocal (max error about 1 ulp); densities never come near
+    // the flush-to-zero range
+    __device__ static float rcp(float a) {
+        float r;
+        asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(a));
+        return r;
+    }
+#else
     __device__ static float rcp(float a) { return __frcp_rn(a); }
+#endif
     __device__ static double add(double a, double b) { return a + b; }
     __device__ static double sub(double a, double b) { return a - b; }
     __device__ static double mul(double a, double b) { return a * b; }

@@ -102,6 +102,21 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t phase,
     return false;
 }
 
+// Arms *bar for `bytes` of asynchronous copies (the arrival of this thread).
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+                 :: "r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+// ---- bulk copy (TMA, non-tensor) -----------------------------------------
+// Global -> shared copy of `bytes` (a multiple of 16; both addresses 16-byte
+// aligned) completing on *bar's transaction count.
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+        :: "r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar)) : "memory");
+}
+
 // ---- TMEM -> registers --------------------------------------------------
 // Each warp of the CTA reads its own 32 TMEM lanes (lane offset in the
 // address's upper half), 32 consecutive 32-bit columns.

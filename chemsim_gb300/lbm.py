@@ -146,6 +146,14 @@ class Lattice:
         check(self._lib.lbm_read_moments(self._h, ctypes.c_void_p(rho_ptr),
                                          ctypes.c_void_p(ux_ptr), ctypes.c_void_p(uy_ptr), 1))
 
+    def save(self, path: str):
+        """Checkpoint: exact state, geometry and parameters (lbm_save)."""
+        check(self._lib.lbm_save(self._h, str(path).encode()))
+
+    def load(self, path: str):
+        """Resume from a checkpoint of a lattice of this size and precision."""
+        check(self._lib.lbm_load(self._h, str(path).encode()))
+
     def render(self, mode: int = 0, geometry_overlay: bool = True) -> np.ndarray:
         """RGBA8 image (h, w, 4) of a moment field coloured as src/render.rs
         does (mode: RENDER_DENSITY, RENDER_SPEED, RENDER_VELOCITY,

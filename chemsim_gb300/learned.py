@@ -77,6 +77,12 @@ class CorrectionNet:
                                            float(lr), ctypes.byref(loss)))
         return float(loss.value)
 
+    def save(self, path: str):
+        check(self._lib.lbm_cnn_save(self._n, str(path).encode()))
+
+    def load(self, path: str):
+        check(self._lib.lbm_cnn_load(self._n, str(path).encode()))
+
     def set_stream(self, stream_ptr: int | None):
         """Issue the net's work on this cudaStream_t (None: its own stream)."""
         check(self._lib.lbm_cnn_set_stream(self._n, ctypes.c_void_p(stream_ptr or 0)))
@@ -99,6 +105,17 @@ def apply_correction(lat, corr, image: int, scale: float, max_abs: float = 0.0):
 
 def target(ref, cur, t, image: int, scale: float):
     check(_lib.load().lbm_coarse_target(ref.handle, cur.handle, float(scale), int(image), _ptr(t)))
+
+
+def coarse_run(lat, net, nsteps: int, k: int, s_rho: float, s_u: float, scale: float,
+               max_abs: float = 0.0, check_every: int = 16, mass_tolerance: float = 1e-3):
+    """lbm_coarse_run: nsteps corrected coarse steps; returns the step count at
+    which the periodic check asked for the fine-grid fallback, or None."""
+    out = ctypes.c_int64()
+    check(_lib.load().lbm_coarse_run(lat.handle, net._n, int(nsteps), int(k), float(s_rho),
+                                     float(s_u), float(scale), float(max_abs), int(check_every),
+                                     float(mass_tolerance), ctypes.byref(out)))
+    return None if out.value < 0 else int(out.value)
 
 
 # ---------------------------------------------------------------------------
@@ -136,9 +153,10 @@ class CorrectionConfig:
     eval_seed: int = 9999
     checkpoints: int = 10
     mass_tolerance: float = 1e-3
-    gain: float = 1.0             # fraction of the predicted correction applied
+    check_every: int = 16         # corrections between health checks of a corrected run
+    gain: float = 0.1             # fraction of the predicted correction applied
     clip: float = 4.0             # |d_i| limit in RMS of the training targets (0: none)
-    data_policy: str = "none"     # first data pass: "none" (coarse-only run) or "teacher"
+    data_policy: str = "teacher"  # first data pass: "teacher" or "none" (coarse-only run)
     onpolicy_passes: int = 0      # data passes with the network's own corrections applied
     onpolicy_iters: int = 1500
     extra: dict = field(default_factory=dict)
@@ -313,18 +331,18 @@ def train_correction(cfg: CorrectionConfig, stream, log=None):
 
 
 def evaluate_correction(cfg: CorrectionConfig, net, s_eff: float, stream, gains=(1.0,),
-                        log=None, trace_every: int = 0) -> dict:
+                        log=None) -> dict:
     """Fine, coarse-only and coarse-plus-correction runs (one per gain) of a
     held-out geometry, side by side on one stream; velocity L2 errors of the
-    coarse runs against the block-averaged fine run at each checkpoint, the
-    time of each run (CUDA events), and the first checkpoint at which a
-    corrected run failed its health check (mass drift or instability) — the
-    point where a production run would fall back to the fine grid."""
+    coarse runs against the block-averaged fine run at each checkpoint and the
+    time of each run (CUDA events).  A corrected run goes through
+    lbm_coarse_run, whose periodic health check (mass drift or instability)
+    hands the run over to the fine grid: from then on it is charged the fine
+    run's time and carries the fine state."""
     import torch
     from . import lbm
     say = log or (lambda *a: None)
     nf, nc, fac = cfg.fine, cfg.coarse, cfg.factor
-    dev = torch.device("cuda")
     (es,), (cs,) = _coarse_specs(cfg, [cfg.eval_seed])
     fluid_c = cs.solid == 0
     flags = es.flags | lbm.FAST
@@ -343,9 +361,6 @@ def evaluate_correction(cfg: CorrectionConfig, net, s_eff: float, stream, gains=
         restrict(fine, lat, fac)
     chunk_f = cfg.horizon_fine // cfg.checkpoints
     chunk_c = chunk_f // fac
-    with torch.cuda.stream(stream):
-        x1 = torch.zeros((1, 4, nc, nc), device=dev)
-        o1 = torch.zeros((1, 9, nc, nc), device=dev)
     stream.synchronize()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
@@ -360,36 +375,26 @@ def evaluate_correction(cfg: CorrectionConfig, net, s_eff: float, stream, gains=
     t_corr = [0.0] * len(gains)
     err_base, err_corr = [], [[] for _ in gains]
     fallback_at = [None] * len(gains)
-    mass0 = [c.health()["mass"] for c in corrs]
-    trace = []
-    ncorr = 0
     for cp in range(cfg.checkpoints):
-        t_fine += timed(lambda: fine.step(chunk_f))
+        t_chunk = timed(lambda: fine.step(chunk_f))
+        t_fine += t_chunk
         t_base += timed(lambda: base.step(chunk_c))
         for g, (gain, corr) in enumerate(zip(gains, corrs)):
+            if fallback_at[g] is not None:
+                # that run has handed over to the fine grid: it costs the fine
+                # chunk and carries the fine state
+                t_corr[g] += t_chunk
+                restrict(fine, corr, fac)
+                continue
+            stop = []
+
             def run():
-                nonlocal ncorr
-                done = 0
-                while done < chunk_c:
-                    n = min(cfg.k, chunk_c - done)
-                    corr.step(n)
-                    done += n
-                    if n == cfg.k:
-                        features(corr, x1, 0, cfg.s_rho, cfg.s_u)
-                        net.forward(x1, o1)
-                        apply_correction(corr, o1, 0, s_eff * gain, cfg.clip * s_eff)
-                        if trace_every and g == 0:
-                            ncorr += 1
-                            if ncorr % trace_every == 0:
-                                trace.append({"correction": ncorr,
-                                              "out_abs_max": float(o1.abs().max()),
-                                              "out_rms": float(o1.pow(2).mean().sqrt()),
-                                              "in_abs_max": float(x1[:, :3].abs().max())})
+                stop.append(coarse_run(corr, net, chunk_c, cfg.k, cfg.s_rho, cfg.s_u,
+                                       s_eff * gain, cfg.clip * s_eff, cfg.check_every,
+                                       cfg.mass_tolerance))
             t_corr[g] += timed(run)
-            h = corr.health()
-            if fallback_at[g] is None and (h["unstable"] or
-                                           abs(h["mass"] - mass0[g]) > cfg.mass_tolerance * mass0[g]):
-                fallback_at[g] = (cp + 1) * chunk_f
+            if stop[0] is not None:
+                fallback_at[g] = stop[0] * fac
         rho, ux, uy = fine.moments()
         rx, ry = _block_velocity(rho, ux, uy, es.solid, fac)
         _, bx, by = base.moments()
@@ -412,12 +417,10 @@ def evaluate_correction(cfg: CorrectionConfig, net, s_eff: float, stream, gains=
             "u_l2_final": err_corr[g][-1], "seconds": round(t_corr[g], 4),
             "time_to_solution_ratio": round(t_fine / max(t_corr[g], 1e-12), 2),
             "fallback_triggered_at_fine_step": fallback_at[g]})
-    if trace:
-        out["trace"] = trace
     return out
 
 
-def run_correction_experiment(cfg: CorrectionConfig, log=None, gains=None, trace_every=0) -> dict:
+def run_correction_experiment(cfg: CorrectionConfig, log=None, gains=None) -> dict:
     """Trains the correction (train_correction) and judges it on a held-out
     geometry (evaluate_correction).  Returns a result dict."""
     import torch
@@ -428,8 +431,45 @@ def run_correction_experiment(cfg: CorrectionConfig, log=None, gains=None, trace
     res["training"]["target_rms"] = s_eff
     try:
         res["evaluation"] = evaluate_correction(cfg, net, s_eff, stream,
-                                                gains=gains or (cfg.gain,), log=log,
-                                                trace_every=trace_every)
+                                                gains=gains or (cfg.gain,), log=log)
     finally:
         net.close()
     return res
+
+
+def forward_throughput(images: int = 8, side: int = 512, reps: int = 20) -> dict:
+    """Times the correction network's forward pass on `images` random images
+    of side x side (CUDA events on the net's stream); TFLOP/s counted with the
+    real channel counts (4 -> 32 -> 32 -> 32 -> 9, 3x3 taps)."""
+    import torch
+    stream = torch.cuda.Stream()
+    macs = 9 * (4 * 32 + 32 * 32 + 32 * 32 + 32 * 9)
+    with CorrectionNet(side, side, images, seed=1) as net:
+        net.set_stream(stream.cuda_stream)
+        with torch.cuda.stream(stream):
+            x = torch.randn((images, 4, side, side), device="cuda")
+            out = torch.empty((images, 9, side, side), device="cuda")
+        stream.synchronize()
+        for _ in range(3):
+            net.forward(x, out)
+        start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        start.record(stream)
+        for _ in range(reps):
+            net.forward(x, out)
+        end.record(stream)
+        end.synchronize()
+        secs = start.elapsed_time(end) / 1e3 / reps
+    flops = 2.0 * macs * images * side * side
+    return {"images": images, "side": side, "ms": round(secs * 1e3, 3),
+            "algorithmic_gflop": round(flops / 1e9, 2), "tflops": round(flops / secs / 1e12, 1)}
+
+
+if __name__ == "__main__":
+    # python -m chemsim_gb300.learned forward [images] [side]
+    import json
+    import sys
+    if len(sys.argv) < 2 or sys.argv[1] != "forward":
+        sys.exit("usage: python -m chemsim_gb300.learned forward [images] [side]")
+    n = int(sys.argv[2]) if len(sys.argv) > 2 else 8
+    side = int(sys.argv[3]) if len(sys.argv) > 3 else 512
+    print(json.dumps(forward_throughput(n, side)))

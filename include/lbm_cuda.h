@@ -198,7 +198,8 @@ int lbm_set_tile(lbm_lattice* lat, int cells_per_thread, int rows_per_block);
 
 /* ---- batches of independent lattices ----------------------------------- */
 /* No reference counterpart: many lattices of uneven sizes and relaxation
- * times advanced together by one persistent launch per time step.          */
+ * times advanced together, each time step a few launches (one per non-empty
+ * (tile width, path) work list) over warp work items of all members.       */
 
 typedef struct lbm_batch lbm_batch;
 
@@ -223,9 +224,9 @@ int lbm_batch_destroy(lbm_batch* batch);
 int lbm_batch_size(lbm_batch* batch, int* n);
 int lbm_batch_lattice(lbm_batch* batch, int index, lbm_lattice** out);
 
-/* Advances every member nsteps steps (one persistent launch per step,
- * replayed from a CUDA graph); each member's time and step count advance as
- * with lbm_step.  Asynchronous on the batch's stream.                      */
+/* Advances every member nsteps steps (the per-step launches replayed from a
+ * CUDA graph); each member's time and step count advance as with lbm_step.
+ * Asynchronous on the batch's stream.                                      */
 int lbm_batch_step(lbm_batch* batch, int nsteps);
 int lbm_batch_synchronize(lbm_batch* batch);
 int lbm_batch_set_stream(lbm_batch* batch, void* stream);
@@ -237,6 +238,18 @@ int lbm_batch_set_stream(lbm_batch* batch, void* stream);
  * JSON file cache_path (NULL: no cache).  A cached entry for this GPU and
  * mode is reused without timing.  steps_per_trial <= 0 selects 24.         */
 int lbm_batch_autotune(lbm_batch* batch, const char* cache_path, int steps_per_trial);
+
+/* ---- checkpoint / resume --------------------------------------------------
+ * A 96-byte header (magic "LBMSTATE", version 1, w, h, precision, flags,
+ * collision, has_solid, tau, tau_minus, dx, dt, fx, fy, time, steps), then
+ * the nine population planes in the lattice's storage type (row-major
+ * y * w + x; 16-bit storage keeps its raw deviation values, so save -> load
+ * is exact), then the w * h solid mask when there is one.  lbm_load needs a
+ * lattice of the same size, precision and boundary flags and restores its
+ * state, geometry, force, collision, discretization, LBM_FAST, time and step
+ * count.                                                                     */
+int lbm_save(lbm_lattice* lat, const char* path);
+int lbm_load(lbm_lattice* lat, const char* path);
 
 /* ---- colour map (src/render.rs) ------------------------------------------
  * Renders the lattice's moments into an RGBA8 image of w x h pixels, pixel
@@ -281,6 +294,10 @@ int lbm_cnn_gradients(lbm_cnn* net, const float* in, const float* target, int ba
 /* One Adam step (beta1 0.9, beta2 0.999) on the MSE loss.                  */
 int lbm_cnn_train_step(lbm_cnn* net, const float* in, const float* target, int batch,
                        float lr, float* loss);
+/* Weights to / from a file: "LBMCNN01", int64 parameter count, the f32
+ * parameters in lbm_cnn_get_params order.                                  */
+int lbm_cnn_save(lbm_cnn* net, const char* path);
+int lbm_cnn_load(lbm_cnn* net, const char* path);
 /* Issue the net's work on `stream` (a cudaStream_t; NULL = the net's own
  * stream).  Calls read their input tensors in that stream's order, so a
  * caller that fills them on another stream orders the two itself.          */
@@ -303,6 +320,17 @@ int lbm_coarse_apply(lbm_lattice* lat, const float* corr, int image, float scale
  * them): the population change that moves cur's velocity onto ref's and
  * leaves its density and non-equilibrium part alone.                        */
 int lbm_coarse_target(lbm_lattice* ref, lbm_lattice* cur, float scale, int image, float* target);
+/* The learned coarse run: nsteps steps of an f32 lattice of the network's
+ * size; after every k steps the network maps the lattice's features
+ * (s_rho, s_u as in lbm_coarse_features) to a correction applied with
+ * lbm_coarse_apply(scale, max_abs).  Every check_every corrections (0 =
+ * never) a health check runs; if the lattice is unstable or its mass moved by
+ * more than mass_tolerance (relative), the run stops and *fallback_step is
+ * the lattice's step count at that point (the caller continues on the fine
+ * grid), else *fallback_step = -1.  All work is on the lattice's stream.     */
+int lbm_coarse_run(lbm_lattice* lat, lbm_cnn* net, int nsteps, int k, float s_rho, float s_u,
+                   float scale, float max_abs, int check_every, float mass_tolerance,
+                   int64_t* fallback_step);
 
 #ifdef __cplusplus
 }

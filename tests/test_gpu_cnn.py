@@ -11,8 +11,8 @@ from chemsim_gb300.lbm import F32, FAST, FRAME_XY, SOLID_HALFWAY, X_PERIODIC, Y_
 pytestmark = pytest.mark.gpu
 torch = pytest.importorskip("torch")
 
-from chemsim_gb300.learned import (CorrectionNet, apply_correction, features,  # noqa: E402
-                                   restrict, target)
+from chemsim_gb300.learned import (CorrectionNet, apply_correction, coarse_run,  # noqa: E402
+                                   features, restrict, target)
 
 
 def _rel(a, b):
@@ -161,3 +161,45 @@ def test_features_apply_target(gpu):
         dc = np.clip(d, -2e-4, 2e-4)
         np.testing.assert_allclose(got, np.where(solid[None], fb, fb + dc - w * dc.sum(axis=0)),
                                    rtol=0, atol=3e-7)
+
+
+def test_weights_save_load(gpu, tmp_path):
+    with CorrectionNet(8, 128, 1, seed=1) as a, CorrectionNet(8, 128, 1, seed=2) as b:
+        assert not np.array_equal(a.get_params(), b.get_params())
+        a.save(tmp_path / "w.bin")
+        b.load(tmp_path / "w.bin")
+        assert np.array_equal(a.get_params(), b.get_params())
+        (tmp_path / "bad.bin").write_bytes(b"LBMCNN01" + b"\0" * 8)
+        with pytest.raises(lbm.LBMError):
+            b.load(tmp_path / "bad.bin")
+
+
+def _coarse_pair(seed):
+    spec = _channel(128, 32, seed)
+    flags = X_PERIODIC | Y_WALL | SOLID_HALFWAY | FRAME_XY | FAST
+    lats = []
+    for _ in range(2):
+        lat = Lattice(128, 32, 0.55, F32, flags)
+        lat.set_force(*spec.force)
+        lat.set_geometry(spec.solid)
+        lat.init_equilibrium(spec.rho, spec.ux, spec.uy)
+        lats.append(lat)
+    return lats
+
+
+def test_coarse_run_with_zero_scale_is_plain_stepping(gpu):
+    a, b = _coarse_pair(6)
+    with CorrectionNet(32, 128, 1, seed=3) as net, a, b:
+        assert coarse_run(a, net, 30, 8, 0.0, 100.0, 0.0, check_every=1) is None
+        b.step(30)
+        assert np.array_equal(a.get_populations(), b.get_populations())
+        assert a.time()[1] == 30
+
+
+def test_coarse_run_falls_back_on_a_failed_check(gpu):
+    a, _ = _coarse_pair(7)
+    with CorrectionNet(32, 128, 1, seed=3) as net, a:
+        f = a.get_populations()
+        f[0, 10, 40] = np.nan                # a planted non-finite population
+        a.set_populations(f)
+        assert coarse_run(a, net, 64, 4, 0.0, 100.0, 1e-6, check_every=1) == 4
