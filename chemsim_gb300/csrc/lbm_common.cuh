@@ -192,7 +192,7 @@ struct StepArgs {
 // Strict arithmetic: one IEEE rounding per operation, no contraction; the
 // operation order of src/lbm.rs.  Fast arithmetic: contracted / simplified.
 #ifndef LBM_RCP_APPROX
-#define LBM_RCP_APPROX 0
+#define LBM_RCP_APPROX 1
 #endif
 template <bool FAST> struct Ar;
 template <> struct Ar<false> {
