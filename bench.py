@@ -15,7 +15,9 @@ populations per step) are larger than L2, so no L2 flush is needed.
           fields are uploaded from pinned host memory and, every frame of two
           steps (the reference demo's speed_factor, src/main.rs:393), rho/u are
           read back into pinned host memory (LBMSim::step + render,
-          src/main.rs:128-177).
+          src/main.rs:128-177).  e2e.rendered_frames: the same loop reading
+          back the finished RGBA8 frame of lbm_render instead (the colour map
+          of render.rs on the device).
   fp16    the same lattice with half-precision deviation storage.
   accuracy  rho/u L2 errors of the f32/f16/bf16 runs against the f64 run of
           the same kernel after the same W + K steps.
@@ -338,12 +340,14 @@ def run_ours(args):
                                    np.stack([m64[1][fluid], m64[2][fluid]]))}
         accuracy = {"steps": args.warmup + args.steps, "against": "f64 run of the same kernel",
                     "f32": errs(m32), "f16dev": errs(m16), "bf16dev": errs(mb),
-                    "u_rms_f64": float(np.sqrt(np.mean(m64[1][fluid] ** 2 + m64[2][fluid] ** 2)))}
+                    "u_rms_f64": float(np.sqrt(np.mean(m64[1][fluid] ** 2 + m64[2][fluid] ** 2))),
+                    "taylor_green_1024": accuracy_taylor_green(args.warmup + args.steps)}
     lat32.close()
     lat16.close()
 
     # e2e through the C ABI with pinned host buffers
     e2e = run_e2e(spec, args, torch, dist)
+    e2e["rendered_frames"] = run_e2e(spec, args, torch, dist, readback="frame")
     batch = None if args.no_batch or world > 1 else run_batch(args, torch)
     large = None if args.no_large or world > 1 else run_large(args, torch)
     learned = None if args.no_learned or world > 1 else run_learned(args, torch)
@@ -399,6 +403,29 @@ def run_ours(args):
     if dist is not None:
         dist.destroy_process_group()
     return 0
+
+
+def accuracy_taylor_green(steps):
+    """rho/u L2 of f32, f16-deviation and bf16-deviation storage against the
+    f64 run of the same kernel on a laminar flow: the 1024^2 Taylor-Green
+    vortex (tau 0.8, u0 0.02), where the error is the storage's own and not
+    the phase drift of an unsteady flow."""
+    from chemsim_gb300 import lbm
+    from chemsim_gb300.workloads import taylor_green_spec
+    spec = taylor_green_spec(1024)
+    runs = {}
+    for name, prec in (("f64", lbm.F64), ("f32", lbm.F32), ("f16dev", lbm.F16DEV),
+                       ("bf16dev", lbm.BF16DEV)):
+        lat = make_lattice(spec, prec, spec.flags | lbm.FAST)
+        lat.step(steps)
+        runs[name] = lat.moments()
+        lat.close()
+    r64, x64, y64 = runs["f64"]
+    out = {"steps": steps, "u_rms_f64": float(np.sqrt(np.mean(x64 ** 2 + y64 ** 2)))}
+    for name in ("f32", "f16dev", "bf16dev"):
+        r, x, y = runs[name]
+        out[name] = {"rho_l2": l2_rel(r, r64), "u_l2": l2_rel(np.stack([x, y]), np.stack([x64, y64]))}
+    return out
 
 
 def run_batch(args, torch):
@@ -528,14 +555,18 @@ def run_large(args, torch):
     return out
 
 
-def run_e2e(spec, args, torch, dist):
+def run_e2e(spec, args, torch, dist, readback="moments"):
     """K steps through the C ABI: upload fields from pinned host memory, then
-    frames of 2 steps each followed by a rho/u readback to pinned memory."""
+    frames of 2 steps each followed by a readback to pinned memory: the
+    rho/u fields (readback="moments", what render.rs takes) or the finished
+    RGBA8 velocity frame from lbm_render (readback="frame")."""
     from chemsim_gb300 import lbm
+    from chemsim_gb300._lib import check
     flags = spec.flags | (0 if args.strict else lbm.FAST)
     pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()  # noqa: E731
     rho, ux, uy = pin(spec.rho), pin(spec.ux), pin(spec.uy)
     out = [torch.empty((spec.h, spec.w), dtype=torch.float32).pin_memory().numpy() for _ in range(3)]
+    img = torch.empty((spec.h, spec.w, 4), dtype=torch.uint8).pin_memory().numpy()
     lat = lbm.Lattice(spec.w, spec.h, spec.tau, lbm.F32, flags)
     lat.set_force(*spec.force)
     lat.set_geometry(spec.solid)
@@ -543,17 +574,20 @@ def run_e2e(spec, args, torch, dist):
     lat.step(args.warmup)
     lat.synchronize()
     frames = max(1, args.steps // 2)
+    lib = lat._lib
     if dist is not None:
         dist.barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     lat.init_equilibrium(rho, ux, uy)
     for _ in range(frames):
-        lat.step_moments(2)
-        lib = lat._lib
-        from chemsim_gb300._lib import check
-        check(lib.lbm_read_moments(lat.handle, out[0].ctypes.data, out[1].ctypes.data,
-                                   out[2].ctypes.data, 0))
+        if readback == "moments":
+            lat.step_moments(2)
+            check(lib.lbm_read_moments(lat.handle, out[0].ctypes.data, out[1].ctypes.data,
+                                       out[2].ctypes.data, 0))
+        else:
+            lat.step_moments(2)
+            check(lib.lbm_render(lat.handle, lbm.RENDER_VELOCITY, 1, img.ctypes.data, 0))
     lat.synchronize()
     secs = time.perf_counter() - t0
     if dist is not None:
@@ -564,11 +598,15 @@ def run_e2e(spec, args, torch, dist):
     world = dist.get_world_size() if dist is not None else 1
     cells = spec.w * spec.h
     steps = 2 * frames
+    per_frame = 3 * 4 * cells if readback == "moments" else 4 * cells
     return {"value": round(cells * steps / secs / 1e6 * world, 1), "unit": "MLUPS",
             "h2d_bytes_per_step": int(3 * 4 * cells / steps),
-            "d2h_bytes_per_step": int(3 * 4 * cells / 2),
+            "d2h_bytes_per_step": int(per_frame / 2),
             "frames": frames, "steps_per_frame": 2,
-            "note": "h2d: rho/ux/uy fields once per run, amortised; d2h: rho/ux/uy every frame"}
+            "note": ("h2d: rho/ux/uy fields once per run, amortised; d2h: rho/ux/uy every frame"
+                     if readback == "moments" else
+                     "h2d: rho/ux/uy fields once per run, amortised; d2h: one RGBA8 velocity "
+                     "frame (lbm_render, render.rs colour map) every frame")}
 
 
 def main():

@@ -203,3 +203,19 @@ def test_coarse_run_falls_back_on_a_failed_check(gpu):
         f[0, 10, 40] = np.nan                # a planted non-finite population
         a.set_populations(f)
         assert coarse_run(a, net, 64, 4, 0.0, 100.0, 1e-6, check_every=1) == 4
+
+
+def test_learned_correction_beats_coarse_only(gpu):
+    """The coarse-plus-correction run against the coarse-only run of a held-out
+    geometry (fine 512^2, coarse 128^2, 4000 fine-equivalent steps): the
+    trained correction lowers the velocity L2 error at every checkpoint and
+    the corrected run stays healthy (no fine-grid fallback)."""
+    from chemsim_gb300.learned import CorrectionConfig, run_correction_experiment
+    cfg = CorrectionConfig(fine=512, n_obstacles=8, r_lo=6, r_hi=16, pairs=1000, horizon_fine=4000,
+                           batch=8, buffer=1000, final_iters=800, checkpoints=8, train_lattices=8)
+    res = run_correction_experiment(cfg)
+    ev = res["evaluation"]
+    corr = ev["corrected"][0]
+    print({"coarse_only": ev["u_l2_coarse_only"], "corrected": corr["u_l2"]})
+    assert corr["fallback_triggered_at_fine_step"] is None
+    assert all(c < b for c, b in zip(corr["u_l2"], ev["u_l2_coarse_only"]))
