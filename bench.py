@@ -209,7 +209,8 @@ def cpu_sample(spec, steps, threads, structured=True):
     """The oracle's CPU step on the full lattice, `steps` steps; MLUPS."""
     import oracle
     f0 = oracle.equilibrium(spec.rho, spec.ux, spec.uy)
-    oracle.step(f0[:, :64], 1, tau=spec.tau, flags=spec.flags, solid=spec.solid[:64],
+    oracle.step(f0[:, :64], 1, tau=spec.tau, flags=spec.flags,
+                solid=None if spec.solid is None else spec.solid[:64],
                 force=spec.force, structured=structured, threads=threads)
     t0 = time.perf_counter()
     oracle.step(f0, steps, tau=spec.tau, flags=spec.flags, solid=spec.solid,
@@ -376,6 +377,7 @@ def run_ours(args):
                "sample": f"3 full {spec.w}x{spec.h} time steps ({secs:.1f} s), f32, the oracle's "
                          "op-by-op restatement of lbm.rs's ArrayFire passes, OpenMP",
                "fused_cpu_mlups": round(vf, 3)}
+    config1 = None if (args.no_cpu or rank != 0) else run_config1(torch)
 
     if rank == 0:
         line = {
@@ -391,6 +393,7 @@ def run_ours(args):
             "roofline": roofline,
             "fp16": fp16,
             "accuracy": accuracy,
+            "taylor_green_256": config1,
             "e2e": e2e,
             "gpu_launches": args.steps,
             "clocks": clk,
@@ -403,6 +406,30 @@ def run_ours(args):
     if dist is not None:
         dist.destroy_process_group()
     return 0
+
+
+def run_config1(torch):
+    """The 256^2 periodic Taylor-Green lattice (tau 0.8, 1000 steps): GPU MLUPS
+    (f32, LBM_FAST and strict) and both CPU steppers on the host cores.  Its
+    4.7 MB per step stay in L2, so no HBM roofline applies."""
+    from chemsim_gb300 import lbm
+    from chemsim_gb300.workloads import taylor_green_spec
+    spec = taylor_green_spec(256)
+    steps = 1000
+    out = {"workload": "taylor_green_256x256_tau0.8_periodic", "steps": steps,
+           "l2": "L2-resident (4.7 MB per step): MLUPS only, no HBM roofline"}
+    stream = torch.cuda.Stream()
+    for name, flags in (("gpu_fast_mlups", spec.flags | lbm.FAST), ("gpu_strict_mlups", spec.flags)):
+        lat = make_lattice(spec, lbm.F32, flags)
+        secs = timed_steps(lat, steps, 20, torch, stream)
+        lat.close()
+        out[name] = round(spec.w * spec.h * steps / secs / 1e6, 1)
+    threads = os.cpu_count() or 1
+    out["cpu_cores"] = threads
+    out["cpu_structured_mlups"] = round(cpu_sample(spec, 50, threads, structured=True)[0], 2)
+    out["cpu_fused_mlups"] = round(cpu_sample(spec, 200, threads, structured=False)[0], 2)
+    out["cpu_sample"] = "50 (structured) and 200 (fused) time steps of the same lattice"
+    return out
 
 
 def accuracy_taylor_green(steps):

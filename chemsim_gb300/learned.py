@@ -140,10 +140,10 @@ class CorrectionConfig:
     r_hi: float = 32.0
     k: int = 8                    # coarse steps between corrections
     train_lattices: int = 8
-    pairs: int = 5000             # horizon_fine / (k * factor) intervals x train_lattices
+    pairs: int = 4000             # snapshot pairs: (intervals of k coarse steps) x train_lattices
     horizon_fine: int = 20000     # fine-equivalent steps of the evaluation
     batch: int = 8
-    buffer: int = 2500            # pairs kept for training (evenly thinned)
+    buffer: int = 4000            # pairs kept for training (evenly thinned when fewer)
     final_iters: int = 3000       # Adam iterations
     lr: float = 1e-3
     s_rho: float = 0.0             # density input off: its acoustic part is noise here

@@ -71,3 +71,20 @@ def test_bad_mode_rejected(gpu, flowing):
     lat, _ = flowing
     with pytest.raises(lbm.LBMError):
         lat.render(7)
+
+
+def test_record_writes_the_rendered_frames(gpu, tmp_path):
+    from chemsim_gb300.record import read_png, record
+    spec = _channel(128, 64, 6)
+    flags = X_PERIODIC | Y_WALL | SOLID_HALFWAY | FRAME_XY | FAST
+    with Lattice(128, 64, 0.6, F32, flags) as a, Lattice(128, 64, 0.6, F32, flags) as b:
+        for lat in (a, b):
+            lat.set_force(*spec.force)
+            lat.set_geometry(spec.solid)
+            lat.init_equilibrium(spec.rho, spec.ux, spec.uy)
+        paths = record(a, 3, str(tmp_path / "frame{:03d}.png"), steps_per_frame=5)
+        assert [p[-12:] for p in paths] == ["frame000.png", "frame001.png", "frame002.png"]
+        for p in paths:
+            b.step(5)
+            with open(p, "rb") as fh:
+                assert np.array_equal(read_png(fh.read()), b.render(RENDER_VELOCITY))
