@@ -72,6 +72,7 @@ def parse_args():
                    help="time the reference operation order instead of LBM_FAST")
     p.add_argument("--no-batch", action="store_true", help="skip the 512-lattice batch")
     p.add_argument("--batch-steps", type=int, default=2000)
+    p.add_argument("--batch-lattices", type=int, default=512)
     p.add_argument("--no-large", action="store_true",
                    help="skip the 16384^2 f16 / 8192^2 f32 comparison")
     p.add_argument("--large-steps", type=int, default=500)
@@ -313,17 +314,22 @@ def run_ours(args):
     lat32 = make_lattice(spec, lbm.F32, base_flags)
     clocks.start()
     t32 = timed_steps(lat32, args.steps, args.warmup, torch, stream, dist)
-    # f16 deviation storage
+    # f16 deviation storage (stochastic rounding, the default), and with
+    # round-to-nearest
     lat16 = make_lattice(spec, lbm.F16DEV, base_flags)
     t16 = timed_steps(lat16, args.steps, args.warmup, torch, stream, dist)
+    lat16n = make_lattice(spec, lbm.F16DEV, base_flags | lbm.ROUND_NEAREST)
+    t16n = timed_steps(lat16n, args.steps, args.warmup, torch, stream, dist)
     clk = clocks.stop()
     mlups32 = cells * args.steps / t32 / 1e6 * world
     mlups16 = cells * args.steps / t16 / 1e6 * world
+    mlups16n = cells * args.steps / t16n / 1e6 * world
 
     accuracy = None
     if not args.no_accuracy:
         m32 = lat32.moments()
         m16 = lat16.moments()
+        m16n = lat16n.moments()
         latb = make_lattice(spec, lbm.BF16DEV, base_flags)
         latb.step(args.warmup + args.steps)
         mb = latb.moments()
@@ -340,11 +346,13 @@ def run_ours(args):
                     "u_l2": l2_rel(np.stack([m[1][fluid], m[2][fluid]]),
                                    np.stack([m64[1][fluid], m64[2][fluid]]))}
         accuracy = {"steps": args.warmup + args.steps, "against": "f64 run of the same kernel",
-                    "f32": errs(m32), "f16dev": errs(m16), "bf16dev": errs(mb),
+                    "f32": errs(m32), "f16dev": errs(m16), "f16dev_round_nearest": errs(m16n),
+                    "bf16dev": errs(mb),
                     "u_rms_f64": float(np.sqrt(np.mean(m64[1][fluid] ** 2 + m64[2][fluid] ** 2))),
                     "taylor_green_1024": accuracy_taylor_green(args.warmup + args.steps)}
     lat32.close()
     lat16.close()
+    lat16n.close()
 
     # e2e through the C ABI with pinned host buffers
     e2e = run_e2e(spec, args, torch, dist)
@@ -364,7 +372,10 @@ def run_ours(args):
                 "algorithmic_bytes_per_cell": bpc, "peak_source": peak_kind,
                 "traffic_unit": "GB per launch"}
     fp16 = {"mlups": round(mlups16, 1), "speedup_vs_f32": round(mlups16 / mlups32, 3),
-            "achieved_gbs": round((BYTES_F16 + BYTES_MASK) * cells / (t16 / args.steps) / 1e9, 1)}
+            "achieved_gbs": round((BYTES_F16 + BYTES_MASK) * cells / (t16 / args.steps) / 1e9, 1),
+            "rounding": "stochastic (hashed from the value's bits)",
+            "round_nearest": {"mlups": round(mlups16n, 1),
+                              "speedup_vs_f32": round(mlups16n / mlups32, 3)}}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -441,15 +452,16 @@ def accuracy_taylor_green(steps):
     from chemsim_gb300.workloads import taylor_green_spec
     spec = taylor_green_spec(1024)
     runs = {}
-    for name, prec in (("f64", lbm.F64), ("f32", lbm.F32), ("f16dev", lbm.F16DEV),
-                       ("bf16dev", lbm.BF16DEV)):
-        lat = make_lattice(spec, prec, spec.flags | lbm.FAST)
+    for name, prec, extra in (("f64", lbm.F64, 0), ("f32", lbm.F32, 0), ("f16dev", lbm.F16DEV, 0),
+                              ("f16dev_round_nearest", lbm.F16DEV, lbm.ROUND_NEAREST),
+                              ("bf16dev", lbm.BF16DEV, 0)):
+        lat = make_lattice(spec, prec, spec.flags | lbm.FAST | extra)
         lat.step(steps)
         runs[name] = lat.moments()
         lat.close()
     r64, x64, y64 = runs["f64"]
     out = {"steps": steps, "u_rms_f64": float(np.sqrt(np.mean(x64 ** 2 + y64 ** 2)))}
-    for name in ("f32", "f16dev", "bf16dev"):
+    for name in ("f32", "f16dev", "f16dev_round_nearest", "bf16dev"):
         r, x, y = runs[name]
         out[name] = {"rho_l2": l2_rel(r, r64), "u_l2": l2_rel(np.stack([x, y]), np.stack([x64, y64]))}
     return out
@@ -462,7 +474,7 @@ def run_batch(args, torch):
     import tempfile
     from chemsim_gb300 import lbm
     from chemsim_gb300.workloads import batch_specs
-    specs = batch_specs(512)
+    specs = batch_specs(args.batch_lattices)
     cells = sum(s.w * s.h for s in specs)
     b = lbm.Batch(specs, lbm.FRAME_XY | lbm.FAST)
     for m, sp in zip(b.members, specs):
@@ -490,7 +502,8 @@ def run_batch(args, torch):
     b.close()
     peak, _ = measured_peak_gbs()
     gbs = (BYTES_F32 + BYTES_MASK) * cells * args.batch_steps / secs / 1e9
-    return {"workload": "512 lattices, sides U[64,1024], tau U[0.52,1.0], TG or channel, 0-16 obstacles, f32",
+    return {"workload": f"{args.batch_lattices} lattices, sides U[64,1024], tau U[0.52,1.0], TG or "
+                        "channel, 0-16 obstacles, f32",
             "cells": cells, "steps": args.batch_steps, "mlups": round(cells * args.batch_steps / secs / 1e6, 1),
             "achieved_gbs": round(gbs, 1), "frac": round(gbs / peak, 4),
             "ms_per_step": round(secs / args.batch_steps * 1e3, 4), "autotune_s": round(tune_s, 2),
@@ -545,10 +558,12 @@ def run_large(args, torch):
     flags = CHANNEL_FLAGS | lbm.FAST
     out = {}
     big = circles_mask(16384, 16384, 256, 20.0, 120.0, seed=5)
-    for name, n, prec, bpc in (("f16dev_16384", 16384, lbm.F16DEV, BYTES_F16 + BYTES_MASK),
-                               ("f32_8192", 8192, lbm.F32, BYTES_F32 + BYTES_MASK)):
+    for name, n, prec, bpc, extra in (
+            ("f16dev_16384", 16384, lbm.F16DEV, BYTES_F16 + BYTES_MASK, 0),
+            ("f16dev_16384_round_nearest", 16384, lbm.F16DEV, BYTES_F16 + BYTES_MASK, lbm.ROUND_NEAREST),
+            ("f32_8192", 8192, lbm.F32, BYTES_F32 + BYTES_MASK, 0)):
         solid = np.ascontiguousarray(big[:n, :n])
-        lat = lbm.Lattice(n, n, 0.52, prec, flags)       # starts at rest: rho = 1, u = 0
+        lat = lbm.Lattice(n, n, 0.52, prec, flags | extra)   # starts at rest: rho = 1, u = 0
         lat.set_force(5e-7, 0.0)
         lat.set_geometry(solid)
         stream = torch.cuda.Stream()
@@ -560,22 +575,25 @@ def run_large(args, torch):
                      "achieved_gbs": round(bpc * n * n * args.large_steps / secs / 1e9, 1),
                      "stable": not h["unstable"]}
     out["f16_speedup_vs_f32"] = round(out["f16dev_16384"]["mlups"] / out["f32_8192"]["mlups"], 3)
+    out["f16_round_nearest_speedup_vs_f32"] = round(
+        out["f16dev_16384_round_nearest"]["mlups"] / out["f32_8192"]["mlups"], 3)
     # accuracy on the 1024^2 window
     crop = np.ascontiguousarray(big[:1024, :1024])
     steps = 2000
     res = {}
-    for prec in (lbm.F64, lbm.F32, lbm.F16DEV):
-        lat = lbm.Lattice(1024, 1024, 0.52, prec, flags)
+    for key, prec, extra in (("f64", lbm.F64, 0), ("f32", lbm.F32, 0), ("f16dev", lbm.F16DEV, 0),
+                             ("f16dev_round_nearest", lbm.F16DEV, lbm.ROUND_NEAREST)):
+        lat = lbm.Lattice(1024, 1024, 0.52, prec, flags | extra)
         lat.set_force(5e-7, 0.0)
         lat.set_geometry(crop)
         lat.step(steps)
-        res[prec] = lat.moments()
+        res[key] = lat.moments()
         lat.close()
     fluid = crop == 0
     acc = {}
-    for prec, name in ((lbm.F32, "f32"), (lbm.F16DEV, "f16dev")):
-        r, x, y = res[prec]
-        r6, x6, y6 = res[lbm.F64]
+    for name in ("f32", "f16dev", "f16dev_round_nearest"):
+        r, x, y = res[name]
+        r6, x6, y6 = res["f64"]
         acc[name] = {"rho_l2": l2_rel(r[fluid], r6[fluid]),
                      "u_l2": l2_rel(np.stack([x[fluid], y[fluid]]), np.stack([x6[fluid], y6[fluid]]))}
     out["accuracy_1024_window"] = {"steps": steps, "against": "f64 run of the same kernel", **acc}

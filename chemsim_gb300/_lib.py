@@ -32,6 +32,7 @@ Y_ZEROPAD, Y_PERIODIC, Y_WALL = 0x00, 0x04, 0x08
 SOLID_FULLWAY, SOLID_HALFWAY = 0x00, 0x10
 FRAME_REF, FRAME_XY = 0x00, 0x20
 FAST = 0x40
+ROUND_NEAREST = 0x80
 REFERENCE_FLAGS = 0x00
 # collision
 COLLISION_BGK, COLLISION_TRT = 0, 1

@@ -123,6 +123,7 @@ Consts<CT> make_consts(const lbm_lattice* L) {
         c.cF4[i] = cF * c.inv_cs4;
     }
     c.collision = L->collision;
+    c.stochastic = (L->flags & LBM_ROUND_NEAREST) ? 0 : 1;
     if (L->precision == LBM_F16DEV) { c.dscale = CT(kHalfDevScale); c.dinv = CT(1) / CT(kHalfDevScale); }
     else if (L->precision == LBM_BF16DEV) { c.dscale = CT(kBf16DevScale); c.dinv = CT(1) / CT(kBf16DevScale); }
     else { c.dscale = CT(1); c.dinv = CT(1); }
@@ -468,7 +469,7 @@ int lbm_create(int w, int h, float tau, int precision, int flags, lbm_lattice** 
         return fail(LBM_ERR_INVALID_ARGUMENT, "tau must be finite and > 0");
     const size_t es = elem_size(precision);
     if (!es) return fail(LBM_ERR_INVALID_ARGUMENT, "unknown precision");
-    if ((flags & 3) == 3 || ((flags >> 2) & 3) == 3 || (flags & ~0x7f))
+    if ((flags & 3) == 3 || ((flags >> 2) & 3) == 3 || (flags & ~0xff))
         return fail(LBM_ERR_INVALID_ARGUMENT, "invalid boundary flags");
     int dev = 0;
     LBM_CUDA(cudaGetDevice(&dev));
@@ -802,7 +803,7 @@ int lbm_load(lbm_lattice* L, const char* path) {
     bool ok = std::fread(&hd, sizeof(hd), 1, fp) == 1 && std::memcmp(hd.magic, kStateMagic, 8) == 0 &&
               hd.version == 1;
     if (ok && (hd.w != L->w || hd.h != L->h || hd.precision != L->precision ||
-               (hd.flags & ~LBM_FAST) != (L->flags & ~LBM_FAST))) {
+               (hd.flags & ~(LBM_FAST | LBM_ROUND_NEAREST)) != (L->flags & ~(LBM_FAST | LBM_ROUND_NEAREST)))) {
         std::fclose(fp);
         return fail(LBM_ERR_INVALID_ARGUMENT,
                     "checkpoint size, precision or boundary flags differ from the lattice's");
@@ -825,7 +826,7 @@ int lbm_load(lbm_lattice* L, const char* path) {
                                    size_t(L->pitch) * L->esize, host.data() + i * n, row, row, L->h,
                                    cudaMemcpyHostToDevice, L->stream));
     LBM_CUDA(cudaStreamSynchronize(L->stream));
-    L->flags = (L->flags & ~LBM_FAST) | (hd.flags & LBM_FAST);
+    L->flags = (L->flags & ~(LBM_FAST | LBM_ROUND_NEAREST)) | (hd.flags & (LBM_FAST | LBM_ROUND_NEAREST));
     L->time = hd.time;
     L->steps = hd.steps;
     L->mom_valid = false;

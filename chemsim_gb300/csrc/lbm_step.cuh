@@ -488,7 +488,7 @@ __device__ __forceinline__ void step_interior(const StepArgs<typename Store<S>::
     collide_cells<S, V, FAST>(a.c, f);
     S enc[9][V];
 #pragma unroll
-    for (int i = 0; i < 9; ++i) ST::enc_vec_dom(f[i], enc[i]);
+    for (int i = 0; i < 9; ++i) ST::enc_vec_dom(f[i], enc[i], a.c.stochastic);
     store_cells<S, V, FAST>(a, y, x0, enc);
 }
 
@@ -560,7 +560,7 @@ __device__ __forceinline__ void step_interior_wrap(const StepArgs<typename Store
     collide_cells<S, V, FAST>(a.c, f);
     S enc[9][V];
 #pragma unroll
-    for (int i = 0; i < 9; ++i) ST::enc_vec_dom(f[i], enc[i]);
+    for (int i = 0; i < 9; ++i) ST::enc_vec_dom(f[i], enc[i], a.c.stochastic);
     if (x0 < w) store_cells<S, V, FAST>(a, y, x0, enc);
 }
 
@@ -740,7 +740,7 @@ __device__ __forceinline__ void step_general(const StepArgs<typename Store<S>::C
     S enc[9][V];
     collide_cells<S, V, FAST>(a.c, f);
 #pragma unroll
-    for (int i = 0; i < 9; ++i) ST::enc_vec_dom(f[i], enc[i]);
+    for (int i = 0; i < 9; ++i) ST::enc_vec_dom(f[i], enc[i], a.c.stochastic);
 
     if (own_solid && halfway) {
         // Half-way mode: solid nodes keep their populations.

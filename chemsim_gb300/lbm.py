@@ -23,7 +23,7 @@ import numpy as np
 
 from . import _lib
 from ._lib import (BF16DEV, COLLISION_BGK, COLLISION_TRT, F16DEV, F32, F64,  # noqa: F401
-                   FAST, FRAME_REF, FRAME_XY, REFERENCE_FLAGS, SOLID_FULLWAY,
+                   FAST, FRAME_REF, FRAME_XY, REFERENCE_FLAGS, ROUND_NEAREST, SOLID_FULLWAY,
                    SOLID_HALFWAY, X_PERIODIC, X_WALL, X_ZEROPAD, Y_PERIODIC,
                    Y_WALL, Y_ZEROPAD, LBMError, LBMHealth, check)
 

@@ -70,6 +70,12 @@ extern "C" {
 /* Arithmetic.                                                                   */
 #define LBM_FAST        0x40 /* FMA-contracted, algebraically simplified collision
                                 instead of the reference's operation order        */
+/* 16-bit deviation storage rounds collided values stochastically by default
+ * (a reproducible offset hashed from the value's own bits): round-to-nearest
+ * repeats the same error step after step on a slowly changing field, and
+ * those errors add up.  This flag selects round-to-nearest (faster, less
+ * accurate over long runs).  Ignored by f32 and f64 storage.               */
+#define LBM_ROUND_NEAREST 0x80
 
 /* The exact lbm.rs semantics: zero-padded streaming, full-way bounce-back on
  * solid nodes, the reference frame, the reference's f32 operation order.     */
