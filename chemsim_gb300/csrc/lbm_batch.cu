@@ -37,7 +37,7 @@ struct lbm_batch {
     int par = 0;                      // steps since the table was built, mod 2
     bool built = false;
     int frame = 0, fast = 1;
-    int grid = 0;
+    int grid[6] = {0, 0, 0, 0, 0, 0};  // per list: resident blocks of its kernel x SMs
     cudaStream_t own = nullptr, stream = nullptr;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     int dev = 0;
@@ -189,7 +189,7 @@ cudaError_t launch(lbm_batch* B, int parity) {
     for (int k = 0; k < kLists; ++k) {
         const int n = B->list_off[k + 1] - B->list_off[k];
         if (n == 0) continue;
-        const int grid = std::min(B->grid, (n + kTaskWarps - 1) / kTaskWarps);
+        const int grid = std::min(B->grid[k], (n + kTaskWarps - 1) / kTaskWarps);
         pick_kernel(k, B->frame, B->fast)<<<grid, dim3(32, kTaskWarps), 0, B->stream>>>(
             B->d_members, B->d_tasks + B->list_off[k], n, parity);
         cudaError_t e = cudaGetLastError();
@@ -275,11 +275,17 @@ int lbm_batch_create(int n, const lbm_desc* descs, int flags, lbm_batch** out) {
     // batch steps without any host synchronisation.
     for (lbm_lattice* L : B->members)
         if (int rc = lbm_set_stream(L, B->stream)) return cleanup(rc);
-    int sms = 0, per_sm = 0;
+    // Each list's persistent grid is exactly one wave of its own kernel: the
+    // kernels differ in registers (2 or 3 resident blocks per SM), and a
+    // second partial wave would leave SMs idle at the end of the launch.
+    int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, B->dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pick_kernel(2, B->frame, B->fast),
-                                                  32 * kTaskWarps, 0);
-    B->grid = std::max(1, sms) * std::max(1, per_sm);
+    for (int k = 0; k < kLists; ++k) {
+        int per_sm = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pick_kernel(k, B->frame, B->fast),
+                                                      32 * kTaskWarps, 0);
+        B->grid[k] = std::max(1, sms) * std::max(1, per_sm);
+    }
     *out = B;
     return LBM_OK;
 }
@@ -403,7 +409,7 @@ int lbm_batch_autotune(lbm_batch* B, const char* cache_path, int steps_per_trial
         view.owns = false;
         view.frame = B->frame;
         view.fast = B->fast;
-        view.grid = B->grid;
+        std::copy(B->grid, B->grid + kLists, view.grid);
         view.stream = B->stream;
         view.dev = B->dev;
         struct Saved { void* f; int cur; float time; int64_t steps; int v, rows; };

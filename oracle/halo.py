@@ -1,8 +1,8 @@
 """CPU-rank simulation of a y-slab partition of one lattice — TEST
 INFRASTRUCTURE ONLY.
 
-The design the GPU path would use on several GPUs (the build runs replicas
-only, every box has one GPU): rank r owns rows [r h / n, (r + 1) h / n) of a
+The design the GPU path would use on several GPUs (the library itself steps
+one lattice per GPU; several GPUs run replicas): rank r owns rows [r h / n, (r + 1) h / n) of a
 lattice that is periodic in y, plus one halo row above and below.  Before
 each step a rank sends the boundary rows of the three populations that stream
 across each face (c_y = +1 up, c_y = -1 down, in the XY frame) to its
