@@ -15,9 +15,11 @@ populations per step) are larger than L2, so no L2 flush is needed.
           fields are uploaded from pinned host memory and, every frame of two
           steps (the reference demo's speed_factor, src/main.rs:393), rho/u are
           read back into pinned host memory (LBMSim::step + render,
-          src/main.rs:128-177).  e2e.rendered_frames: the same loop reading
-          back the finished RGBA8 frame of lbm_render instead (the colour map
-          of render.rs on the device).
+          src/main.rs:128-177) with lbm_read_moments_async, whose host copy
+          overlaps the next frame's steps; the last copy is waited for inside
+          the timed region.  e2e.blocking_readback: the same loop with the
+          blocking lbm_read_moments; e2e.rendered_frames: reading back the
+          finished RGBA8 frame of lbm_render (render.rs's colour map).
   fp16    the same lattice with half-precision deviation storage.
   accuracy  rho/u L2 errors of the f32/f16/bf16 runs against the f64 run of
           the same kernel after the same W + K steps.
@@ -356,6 +358,7 @@ def run_ours(args):
 
     # e2e through the C ABI with pinned host buffers
     e2e = run_e2e(spec, args, torch, dist)
+    e2e["blocking_readback"] = run_e2e(spec, args, torch, dist, readback="moments")
     e2e["rendered_frames"] = run_e2e(spec, args, torch, dist, readback="frame")
     batch = None if args.no_batch or world > 1 else run_batch(args, torch)
     large = None if args.no_large or world > 1 else run_large(args, torch)
@@ -600,23 +603,33 @@ def run_large(args, torch):
     return out
 
 
-def run_e2e(spec, args, torch, dist, readback="moments"):
+def run_e2e(spec, args, torch, dist, readback="async"):
     """K steps through the C ABI: upload fields from pinned host memory, then
-    frames of 2 steps each followed by a readback to pinned memory: the
-    rho/u fields (readback="moments", what render.rs takes) or the finished
-    RGBA8 velocity frame from lbm_render (readback="frame")."""
+    frames of 2 steps each followed by a readback to pinned memory:
+      "async"   rho/u (what render.rs takes) with lbm_read_moments_async into
+                two alternating pinned host buffer sets, so each frame's host
+                copy overlaps the next frame's steps; the last one is waited
+                for inside the timed region;
+      "moments" the same fields with the blocking lbm_read_moments;
+      "frame"   the finished RGBA8 velocity frame of lbm_render_async (the
+                colour map of render.rs on the device) into two alternating
+                pinned images, overlapped like "async"."""
     from chemsim_gb300 import lbm
     from chemsim_gb300._lib import check
     flags = spec.flags | (0 if args.strict else lbm.FAST)
     pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()  # noqa: E731
     rho, ux, uy = pin(spec.rho), pin(spec.ux), pin(spec.uy)
-    out = [torch.empty((spec.h, spec.w), dtype=torch.float32).pin_memory().numpy() for _ in range(3)]
-    img = torch.empty((spec.h, spec.w, 4), dtype=torch.uint8).pin_memory().numpy()
+    outs = [[torch.empty((spec.h, spec.w), dtype=torch.float32).pin_memory().numpy()
+             for _ in range(3)] for _ in range(2)]
+    imgs = [torch.empty((spec.h, spec.w, 4), dtype=torch.uint8).pin_memory().numpy()
+            for _ in range(2)]
     lat = lbm.Lattice(spec.w, spec.h, spec.tau, lbm.F32, flags)
     lat.set_force(*spec.force)
     lat.set_geometry(spec.solid)
     lat.init_equilibrium(rho, ux, uy)
     lat.step(args.warmup)
+    lat.read_moments_async(*outs[0])          # allocates the staging area outside the timing
+    lat.readback_wait()
     lat.synchronize()
     frames = max(1, args.steps // 2)
     lib = lat._lib
@@ -625,14 +638,17 @@ def run_e2e(spec, args, torch, dist, readback="moments"):
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     lat.init_equilibrium(rho, ux, uy)
-    for _ in range(frames):
-        if readback == "moments":
-            lat.step_moments(2)
-            check(lib.lbm_read_moments(lat.handle, out[0].ctypes.data, out[1].ctypes.data,
-                                       out[2].ctypes.data, 0))
+    for k in range(frames):
+        lat.step_moments(2)
+        if readback == "async":
+            lat.read_moments_async(*outs[k & 1])
+        elif readback == "moments":
+            o = outs[0]
+            check(lib.lbm_read_moments(lat.handle, o[0].ctypes.data, o[1].ctypes.data,
+                                       o[2].ctypes.data, 0))
         else:
-            lat.step_moments(2)
-            check(lib.lbm_render(lat.handle, lbm.RENDER_VELOCITY, 1, img.ctypes.data, 0))
+            lat.render_async(imgs[k & 1], lbm.RENDER_VELOCITY)
+    lat.readback_wait()
     lat.synchronize()
     secs = time.perf_counter() - t0
     if dist is not None:
@@ -643,15 +659,17 @@ def run_e2e(spec, args, torch, dist, readback="moments"):
     world = dist.get_world_size() if dist is not None else 1
     cells = spec.w * spec.h
     steps = 2 * frames
-    per_frame = 3 * 4 * cells if readback == "moments" else 4 * cells
+    per_frame = 4 * cells if readback == "frame" else 3 * 4 * cells
+    notes = {"async": "rho/ux/uy every frame, lbm_read_moments_async into alternating pinned "
+                      "buffers (copy overlaps the next frame's steps)",
+             "moments": "rho/ux/uy every frame, blocking lbm_read_moments",
+             "frame": "one RGBA8 velocity frame every frame (lbm_render_async, render.rs colour "
+                      "map; copy overlaps the next frame's steps)"}
     return {"value": round(cells * steps / secs / 1e6 * world, 1), "unit": "MLUPS",
             "h2d_bytes_per_step": int(3 * 4 * cells / steps),
             "d2h_bytes_per_step": int(per_frame / 2),
             "frames": frames, "steps_per_frame": 2,
-            "note": ("h2d: rho/ux/uy fields once per run, amortised; d2h: rho/ux/uy every frame"
-                     if readback == "moments" else
-                     "h2d: rho/ux/uy fields once per run, amortised; d2h: one RGBA8 velocity "
-                     "frame (lbm_render, render.rs colour map) every frame")}
+            "note": "h2d: rho/ux/uy fields once per run, amortised; d2h: " + notes[readback]}
 
 
 def main():

@@ -114,7 +114,10 @@ SIGNATURES = {
     "lbm_batch_synchronize": (_i32, [_vp]),
     "lbm_batch_set_stream": (_i32, [_vp, _vp]),
     "lbm_batch_autotune": (_i32, [_vp, ctypes.c_char_p, _i32]),
+    "lbm_read_moments_async": (_i32, [_vp, _vp, _vp, _vp]),
+    "lbm_readback_wait": (_i32, [_vp]),
     "lbm_render": (_i32, [_vp, _i32, _i32, _vp, _i32]),
+    "lbm_render_async": (_i32, [_vp, _i32, _i32, _vp]),
     "lbm_save": (_i32, [_vp, ctypes.c_char_p]),
     "lbm_load": (_i32, [_vp, ctypes.c_char_p]),
     "lbm_cnn_create": (_i32, [_i32, _i32, _i32, ctypes.c_uint64, ctypes.POINTER(_vp)]),

@@ -395,6 +395,15 @@ int lattice_refresh_moments(lbm_lattice* L) {
     return LBM_OK;
 }
 
+int lattice_readback_stream(lbm_lattice* L) {
+    if (L->rb_stream) return LBM_OK;
+    DeviceGuard g(L->dev);
+    LBM_CUDA(cudaStreamCreateWithFlags(&L->rb_stream, cudaStreamNonBlocking));
+    LBM_CUDA(cudaEventCreateWithFlags(&L->rb_staged, cudaEventDisableTiming));
+    LBM_CUDA(cudaEventCreateWithFlags(&L->rb_landed, cudaEventDisableTiming));
+    return LBM_OK;
+}
+
 void lattice_advance(lbm_lattice* L, int nsteps) {
     if (nsteps & 1) L->cur ^= 1;
     for (int k = 0; k < nsteps; ++k) L->time += L->dt;
@@ -523,6 +532,11 @@ int lbm_destroy(lbm_lattice* L) {
         if (L->staging) cudaFree(L->staging);
         if (L->health) cudaFree(L->health);
         if (L->render) cudaFree(L->render);
+        if (L->rb_stream) cudaStreamSynchronize(L->rb_stream);
+        if (L->rb) cudaFree(L->rb);
+        if (L->rb_stream) cudaStreamDestroy(L->rb_stream);
+        if (L->rb_staged) cudaEventDestroy(L->rb_staged);
+        if (L->rb_landed) cudaEventDestroy(L->rb_landed);
         if (L->tflags) cudaFree(L->tflags);
         if (L->gtiles) cudaFree(L->gtiles);
         if (L->own) cudaStreamDestroy(L->own);
@@ -679,6 +693,46 @@ int lbm_read_moments(lbm_lattice* L, float* rho, float* ux, float* uy, int on_de
         LBM_CUDA(cudaMemcpy2DAsync(dst[m], size_t(L->w) * 4, L->mom[m], size_t(L->pitch) * 4,
                                    size_t(L->w) * 4, L->h, kind, L->stream));
     LBM_CUDA(cudaStreamSynchronize(L->stream));
+    return LBM_OK;
+}
+
+int lbm_read_moments_async(lbm_lattice* L, float* rho, float* ux, float* uy) {
+    if (int rc = check_handle(L)) return rc;
+    if (!rho || !ux || !uy) return fail(LBM_ERR_INVALID_ARGUMENT, "null field pointer");
+    DeviceGuard g(L->dev);
+    const size_t plane = size_t(L->w) * L->h;
+    if (int rc = lattice_readback_stream(L)) return rc;
+    if (!L->rb) {
+        if (L->rb_pending) LBM_CUDA(cudaEventSynchronize(L->rb_landed));
+        LBM_CUDA(cudaMalloc(reinterpret_cast<void**>(&L->rb), 3 * plane * sizeof(float)));
+    }
+    if (!L->mom_valid) {
+        if (int rc = LBM_DISPATCH(L, moments_t, L)) return rc;
+        L->mom_valid = true;
+    }
+    // the staging area is reused: its previous host copy must have finished
+    if (L->rb_pending) LBM_CUDA(cudaStreamWaitEvent(L->stream, L->rb_landed, 0));
+    for (int m = 0; m < 3; ++m)
+        LBM_CUDA(cudaMemcpy2DAsync(L->rb + m * plane, size_t(L->w) * 4, L->mom[m],
+                                   size_t(L->pitch) * 4, size_t(L->w) * 4, L->h,
+                                   cudaMemcpyDeviceToDevice, L->stream));
+    LBM_CUDA(cudaEventRecord(L->rb_staged, L->stream));
+    LBM_CUDA(cudaStreamWaitEvent(L->rb_stream, L->rb_staged, 0));
+    float* dst[3] = {rho, ux, uy};
+    for (int m = 0; m < 3; ++m)
+        LBM_CUDA(cudaMemcpyAsync(dst[m], L->rb + m * plane, plane * sizeof(float),
+                                 cudaMemcpyDeviceToHost, L->rb_stream));
+    LBM_CUDA(cudaEventRecord(L->rb_landed, L->rb_stream));
+    L->rb_pending = true;
+    return LBM_OK;
+}
+
+int lbm_readback_wait(lbm_lattice* L) {
+    if (int rc = check_handle(L)) return rc;
+    if (!L->rb_pending) return LBM_OK;
+    DeviceGuard g(L->dev);
+    LBM_CUDA(cudaEventSynchronize(L->rb_landed));
+    L->rb_pending = false;
     return LBM_OK;
 }
 

@@ -22,6 +22,10 @@ struct lbm_lattice {
     lbmk::HealthPartial* health = nullptr;  // kHealthBlocks partials + 1 result
     void* render = nullptr;               // colour-map scratch (stats, host-bound image)
     size_t render_bytes = 0;
+    float* rb = nullptr;                  // staged moments of an asynchronous readback
+    cudaStream_t rb_stream = nullptr;     // its device-to-host copies
+    cudaEvent_t rb_staged = nullptr, rb_landed = nullptr;
+    bool rb_pending = false;
     uint8_t* tflags = nullptr;            // h x ceil(w / 32) bytes
     int ntiles = 0;
     uint32_t* gtiles = nullptr;           // list of flagged tiles
@@ -51,6 +55,9 @@ void lattice_advance(lbm_lattice* L, int nsteps);
 
 // Brings L's moment buffers (rho, ux, uy) up to date with its state.
 int lattice_refresh_moments(lbm_lattice* L);
+
+// Creates the stream and events of asynchronous readbacks (once).
+int lattice_readback_stream(lbm_lattice* L);
 
 // Records msg for lbm_last_error_string and returns code.
 int lattice_fail(int code, const std::string& msg);

@@ -156,34 +156,37 @@ render_pixels_kernel(RenderField f, const double* __restrict__ stats,
 
 }  // namespace
 
-extern "C" int lbm_render(lbm_lattice* L, int mode, int geometry_overlay, uint8_t* rgba,
-                          int on_device) {
+namespace {
+
+int cuda_status(cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return LBM_OK;
+    (void)cudaGetLastError();
+    return lbmk::lattice_fail(e == cudaErrorMemoryAllocation ? LBM_ERR_OUT_OF_MEMORY : LBM_ERR_CUDA,
+                              std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+// Renders into dev_out (a device image), or into the lattice's own image
+// buffer when dev_out is null (returned in *img_out); all on L's stream.
+int render_launch(lbm_lattice* L, int mode, int geometry_overlay, uchar4* dev_out, uchar4** img_out) {
     using lbmk::lattice_fail;
-    if (!L) return lattice_fail(LBM_ERR_INVALID_ARGUMENT, "null lattice");
-    if (!rgba) return lattice_fail(LBM_ERR_INVALID_ARGUMENT, "null image pointer");
     if (mode < LBM_RENDER_DENSITY || mode > LBM_RENDER_MOMENTUM)
         return lattice_fail(LBM_ERR_INVALID_ARGUMENT, "unknown render mode");
     if (cudaSetDevice(L->dev) != cudaSuccess) return lattice_fail(LBM_ERR_CUDA, "cudaSetDevice");
     if (int rc = lbmk::lattice_refresh_moments(L)) return rc;
     const size_t img = size_t(L->w) * L->h * 4;
-    const size_t need = (on_device ? 0 : img) + (kRenderBlocks + 2) * sizeof(double);
-    auto cuda = [&](cudaError_t e, const char* what) -> int {
-        if (e == cudaSuccess) return LBM_OK;
-        (void)cudaGetLastError();
-        return lattice_fail(e == cudaErrorMemoryAllocation ? LBM_ERR_OUT_OF_MEMORY : LBM_ERR_CUDA,
-                            std::string(what) + ": " + cudaGetErrorString(e));
-    };
+    const size_t need = (dev_out ? 0 : img) + (kRenderBlocks + 2) * sizeof(double);
     if (L->render_bytes < need) {
+        if (L->rb_pending)                 // an asynchronous frame may still be reading it
+            if (int rc = cuda_status(cudaEventSynchronize(L->rb_landed), "cudaEventSynchronize")) return rc;
         if (L->render) cudaFree(L->render);
         L->render = nullptr;
         L->render_bytes = 0;
-        if (int rc = cuda(cudaMalloc(&L->render, need), "cudaMalloc")) return rc;
+        if (int rc = cuda_status(cudaMalloc(&L->render, need), "cudaMalloc")) return rc;
         L->render_bytes = need;
     }
     double* partial = static_cast<double*>(L->render);
     double* stats = partial + kRenderBlocks;
-    uchar4* out = on_device ? reinterpret_cast<uchar4*>(rgba)
-                            : reinterpret_cast<uchar4*>(stats + 2);
+    uchar4* out = dev_out ? dev_out : reinterpret_cast<uchar4*>(stats + 2);
     const RenderField f{L->mom[0], L->mom[1], L->mom[2], L->pitch, L->w, L->h, mode};
     const int64_t n = int64_t(L->w) * L->h;
     for (int pass = 0; pass < 2; ++pass) {
@@ -193,10 +196,50 @@ extern "C" int lbm_render(lbm_lattice* L, int mode, int geometry_overlay, uint8_
     const int64_t blocks = std::min<int64_t>((n + kRenderThreads - 1) / kRenderThreads, 65535 * 8);
     render_pixels_kernel<<<int(blocks), kRenderThreads, 0, L->stream>>>(
         f, stats, (geometry_overlay && L->has_solid) ? L->solid : nullptr, L->mpitch, out);
-    if (int rc = cuda(cudaGetLastError(), "render launch")) return rc;
+    if (img_out) *img_out = out;
+    return cuda_status(cudaGetLastError(), "render launch");
+}
+
+}  // namespace
+
+extern "C" int lbm_render(lbm_lattice* L, int mode, int geometry_overlay, uint8_t* rgba,
+                          int on_device) {
+    using lbmk::lattice_fail;
+    if (!L) return lattice_fail(LBM_ERR_INVALID_ARGUMENT, "null lattice");
+    if (!rgba) return lattice_fail(LBM_ERR_INVALID_ARGUMENT, "null image pointer");
+    if (L->rb_pending && !on_device)   // the lattice's image buffer may be in flight
+        if (int rc = cuda_status(cudaStreamWaitEvent(L->stream, L->rb_landed, 0), "wait")) return rc;
+    uchar4* out = nullptr;
+    if (int rc = render_launch(L, mode, geometry_overlay,
+                               on_device ? reinterpret_cast<uchar4*>(rgba) : nullptr, &out))
+        return rc;
     if (!on_device)
-        if (int rc = cuda(cudaMemcpyAsync(rgba, out, img, cudaMemcpyDeviceToHost, L->stream),
-                          "cudaMemcpyAsync"))
+        if (int rc = cuda_status(cudaMemcpyAsync(rgba, out, size_t(L->w) * L->h * 4,
+                                                 cudaMemcpyDeviceToHost, L->stream),
+                                 "cudaMemcpyAsync"))
             return rc;
-    return cuda(cudaStreamSynchronize(L->stream), "cudaStreamSynchronize");
+    return cuda_status(cudaStreamSynchronize(L->stream), "cudaStreamSynchronize");
+}
+
+// The frame rendered on the lattice's stream, copied to the host on the
+// readback stream without waiting (see lbm_read_moments_async).
+extern "C" int lbm_render_async(lbm_lattice* L, int mode, int geometry_overlay, uint8_t* rgba) {
+    using lbmk::lattice_fail;
+    if (!L) return lattice_fail(LBM_ERR_INVALID_ARGUMENT, "null lattice");
+    if (!rgba) return lattice_fail(LBM_ERR_INVALID_ARGUMENT, "null image pointer");
+    if (int rc = lbmk::lattice_readback_stream(L)) return rc;
+    // the image buffer is reused: its previous host copy must have finished
+    if (L->rb_pending)
+        if (int rc = cuda_status(cudaStreamWaitEvent(L->stream, L->rb_landed, 0), "wait")) return rc;
+    uchar4* out = nullptr;
+    if (int rc = render_launch(L, mode, geometry_overlay, nullptr, &out)) return rc;
+    if (int rc = cuda_status(cudaEventRecord(L->rb_staged, L->stream), "record")) return rc;
+    if (int rc = cuda_status(cudaStreamWaitEvent(L->rb_stream, L->rb_staged, 0), "wait")) return rc;
+    if (int rc = cuda_status(cudaMemcpyAsync(rgba, out, size_t(L->w) * L->h * 4,
+                                             cudaMemcpyDeviceToHost, L->rb_stream),
+                             "cudaMemcpyAsync"))
+        return rc;
+    if (int rc = cuda_status(cudaEventRecord(L->rb_landed, L->rb_stream), "record")) return rc;
+    L->rb_pending = true;
+    return LBM_OK;
 }

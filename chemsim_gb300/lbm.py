@@ -142,6 +142,18 @@ class Lattice:
         check(self._lib.lbm_read_moments(self._h, _f32ptr(rho), _f32ptr(ux), _f32ptr(uy), 0))
         return rho, ux, uy
 
+    def read_moments_async(self, rho: np.ndarray, ux: np.ndarray, uy: np.ndarray):
+        """Starts copying rho/u into these (h, w) float32 host arrays (pinned for
+        overlap); they hold the fields of the current step once
+        readback_wait() returns (lbm_read_moments_async)."""
+        for a in (rho, ux, uy):
+            if a.dtype != np.float32 or a.shape != (self.h, self.w) or not a.flags.c_contiguous:
+                raise ValueError("expected contiguous (h, w) float32 arrays")
+        check(self._lib.lbm_read_moments_async(self._h, _f32ptr(rho), _f32ptr(ux), _f32ptr(uy)))
+
+    def readback_wait(self):
+        check(self._lib.lbm_readback_wait(self._h))
+
     def moments_to_device(self, rho_ptr: int, ux_ptr: int, uy_ptr: int):
         check(self._lib.lbm_read_moments(self._h, ctypes.c_void_p(rho_ptr),
                                          ctypes.c_void_p(ux_ptr), ctypes.c_void_p(uy_ptr), 1))
@@ -162,6 +174,14 @@ class Lattice:
         check(self._lib.lbm_render(self._h, int(mode), int(bool(geometry_overlay)),
                                    img.ctypes.data_as(ctypes.c_void_p), 0))
         return img
+
+    def render_async(self, img: np.ndarray, mode: int = 0, geometry_overlay: bool = True):
+        """Starts rendering into this (h, w, 4) uint8 host array (pinned for
+        overlap); it holds the frame once readback_wait() returns."""
+        if img.dtype != np.uint8 or img.shape != (self.h, self.w, 4) or not img.flags.c_contiguous:
+            raise ValueError("expected a contiguous (h, w, 4) uint8 array")
+        check(self._lib.lbm_render_async(self._h, int(mode), int(bool(geometry_overlay)),
+                                         img.ctypes.data_as(ctypes.c_void_p)))
 
     def render_to_device(self, rgba_ptr: int, mode: int = 0, geometry_overlay: bool = True):
         check(self._lib.lbm_render(self._h, int(mode), int(bool(geometry_overlay)),

@@ -160,6 +160,15 @@ int lbm_step_moments(lbm_lattice* lat, int nsteps);
  * pointers.  Synchronises the handle's stream.                           */
 int lbm_read_moments(lbm_lattice* lat, float* rho, float* ux, float* uy,
                      int on_device);
+/* The same fields copied to host memory without waiting, for render loops:
+ * they are staged on the device in the lattice's stream order (a
+ * device-to-device copy), then copied to the host on a second stream, so
+ * following steps run while that copy is in flight.  The host buffers
+ * (pinned, for the copy to overlap) must stay valid and unread until
+ * lbm_readback_wait returns.  One readback is in flight at a time: the next
+ * one's staging waits on the device for the previous host copy.            */
+int lbm_read_moments_async(lbm_lattice* lat, float* rho, float* ux, float* uy);
+int lbm_readback_wait(lbm_lattice* lat);
 
 /* Health check (see lbm_health).  Synchronises the handle's stream.      */
 int lbm_check(lbm_lattice* lat, lbm_health* out);
@@ -272,6 +281,10 @@ int lbm_load(lbm_lattice* lat, const char* path);
 #define LBM_RENDER_VELOCITY 2
 #define LBM_RENDER_MOMENTUM 3
 int lbm_render(lbm_lattice* lat, int mode, int geometry_overlay, uint8_t* rgba, int on_device);
+/* The same frame copied to host memory without waiting, like
+ * lbm_read_moments_async (and sharing its one-in-flight readback): rgba
+ * (pinned, for overlap) holds the frame once lbm_readback_wait returns.    */
+int lbm_render_async(lbm_lattice* lat, int mode, int geometry_overlay, uint8_t* rgba);
 
 /* ---- learned coarse-grid correction --------------------------------------
  * No reference counterpart.  A 4-layer 3x3 convolutional network (channels

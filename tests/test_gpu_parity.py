@@ -425,3 +425,35 @@ def test_stochastic_rounding_of_16bit_storage(gpu):
     assert u_err(m_sr) * 3 < u_err(m_rn)
     _, f_again = run(F16DEV)
     assert np.array_equal(f_sr, f_again)
+
+
+def test_async_moment_readback_is_a_snapshot(gpu):
+    """lbm_read_moments_async returns the fields of the step it was called
+    at, even when steps run while the host copy is in flight."""
+    import torch
+    spec = channel_spec(256, n_obstacles=3, r_lo=5, r_hi=10, force=1e-5, seed=4, h=128)
+    flags = spec.flags | FAST
+
+    def lattice():
+        lat = Lattice(spec.w, spec.h, spec.tau, F32, flags)
+        lat.set_force(*spec.force)
+        lat.set_geometry(spec.solid)
+        lat.init_equilibrium(spec.rho, spec.ux, spec.uy)
+        return lat
+
+    pin = [torch.empty((spec.h, spec.w), dtype=torch.float32).pin_memory().numpy() for _ in range(3)]
+    with lattice() as a, lattice() as b:
+        a.step(10)
+        a.read_moments_async(*pin)
+        a.step(7)                       # runs while the copy may still be in flight
+        a.readback_wait()
+        b.step(10)
+        rho, ux, uy = b.moments()
+        assert np.array_equal(pin[0], rho) and np.array_equal(pin[1], ux) and np.array_equal(pin[2], uy)
+        a.synchronize()
+        assert a.time()[1] == 17
+        # back to back: the second readback waits for the first one's copy
+        a.read_moments_async(*pin)
+        a.readback_wait()
+        b.step(7)
+        assert np.array_equal(pin[1], b.moments()[1])

@@ -88,3 +88,24 @@ def test_record_writes_the_rendered_frames(gpu, tmp_path):
             b.step(5)
             with open(p, "rb") as fh:
                 assert np.array_equal(read_png(fh.read()), b.render(RENDER_VELOCITY))
+
+
+def test_render_async_is_a_snapshot(gpu):
+    torch = pytest.importorskip("torch")
+    spec = _channel(128, 64, 7)
+    flags = X_PERIODIC | Y_WALL | SOLID_HALFWAY | FRAME_XY | FAST
+    with Lattice(128, 64, 0.6, F32, flags) as a, Lattice(128, 64, 0.6, F32, flags) as b:
+        for lat in (a, b):
+            lat.set_force(*spec.force)
+            lat.set_geometry(spec.solid)
+            lat.init_equilibrium(spec.rho, spec.ux, spec.uy)
+        imgs = [torch.zeros((64, 128, 4), dtype=torch.uint8).pin_memory().numpy() for _ in range(2)]
+        a.step(6)
+        a.render_async(imgs[0], RENDER_SPEED)
+        a.step(6)                       # runs while the copy may be in flight
+        a.render_async(imgs[1], RENDER_SPEED)
+        a.readback_wait()
+        b.step(6)
+        assert np.array_equal(imgs[0], b.render(RENDER_SPEED))
+        b.step(6)
+        assert np.array_equal(imgs[1], b.render(RENDER_SPEED))
