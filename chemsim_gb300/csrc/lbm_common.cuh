@@ -124,13 +124,12 @@ struct DevStore {
         }
     }
     // Stores the collided values.  With `stochastic` each value is rounded
-    // stochastically: a pseudo-random offset below the 16-bit format's last
-    // place (a multiplicative hash of the value's own f32 bits, so the result
-    // is reproducible) is added before truncation.  Rounding to nearest
-    // repeats the same error on a slowly changing field step after step, and
-    // those errors add up; with the offset they average out (the u error of a
-    // laminar 1024^2 Taylor-Green run after 5000 steps drops from 1.6e-2 to
-    // 7e-4 against f64).
+    // stochastically (the hardware conversion, random bits hashed from the
+    // values' own f32 bits, so the result is reproducible).  Rounding to
+    // nearest repeats the same error on a slowly changing field step after
+    // step, and those errors add up; stochastic rounding averages them out
+    // (the u error of a laminar 1024^2 Taylor-Green run after 5000 steps
+    // drops from 1.6e-2 to 7e-4 against f64).
     template <int V>
     __device__ static void enc_vec_dom(const float (&f)[V], H (&s)[V], int stochastic) {
 #pragma unroll
@@ -142,14 +141,6 @@ struct DevStore {
     __device__ static H2 from_f2_sr(float lo, float hi);
 };
 
-// The f32 bits of v plus an offset of `drop` random low bits (the bits the
-// 16-bit format drops), left alone for Inf/NaN.
-template <int DROP>
-__device__ __forceinline__ float sr_offset(float v) {
-    const uint32_t b = __float_as_uint(v);
-    const uint32_t r = (b * 0x9E3779B1u) >> (32 - DROP);
-    return __uint_as_float((b & 0x7F800000u) == 0x7F800000u ? b : b + r);
-}
 template <> __device__ inline float DevStore<__half, __half2>::to_f(__half s) { return __half2float(s); }
 template <> __device__ inline __half DevStore<__half, __half2>::from_f(float f) { return __float2half_rn(f); }
 template <> __device__ inline float2 DevStore<__half, __half2>::to_f2(__half2 s) { return __half22float2(s); }
@@ -158,10 +149,16 @@ template <> __device__ inline float DevStore<__nv_bfloat16, __nv_bfloat162>::to_
 template <> __device__ inline __nv_bfloat16 DevStore<__nv_bfloat16, __nv_bfloat162>::from_f(float f) { return __float2bfloat16_rn(f); }
 template <> __device__ inline float2 DevStore<__nv_bfloat16, __nv_bfloat162>::to_f2(__nv_bfloat162 s) { return __bfloat1622float2(s); }
 template <> __device__ inline __nv_bfloat162 DevStore<__nv_bfloat16, __nv_bfloat162>::from_f2(float2 f) { return __float22bfloat162_rn(f); }
+// Random bits of a pair for the stochastic-rounding conversion: multiplicative
+// hashes of both values' f32 bits, so a run is reproducible bit for bit.
+__device__ __forceinline__ uint32_t sr_bits(float lo, float hi) {
+    return (__float_as_uint(lo) * 0x9E3779B1u) ^ (__float_as_uint(hi) * 0x85EBCA77u);
+}
+// cvt.rs: the hardware stochastic-rounding conversion of sm_100-class GPUs.
 template <>
 __device__ inline __half2 DevStore<__half, __half2>::from_f2_sr(float lo, float hi) {
     uint32_t d;
-    asm("cvt.rz.f16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(sr_offset<13>(hi)), "f"(sr_offset<13>(lo)));
+    asm("cvt.rs.f16x2.f32 %0, %1, %2, %3;" : "=r"(d) : "f"(hi), "f"(lo), "r"(sr_bits(lo, hi)));
     __half2 out;
     memcpy(&out, &d, 4);
     return out;
@@ -169,7 +166,7 @@ __device__ inline __half2 DevStore<__half, __half2>::from_f2_sr(float lo, float 
 template <>
 __device__ inline __nv_bfloat162 DevStore<__nv_bfloat16, __nv_bfloat162>::from_f2_sr(float lo, float hi) {
     uint32_t d;
-    asm("cvt.rz.bf16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(sr_offset<16>(hi)), "f"(sr_offset<16>(lo)));
+    asm("cvt.rs.bf16x2.f32 %0, %1, %2, %3;" : "=r"(d) : "f"(hi), "f"(lo), "r"(sr_bits(lo, hi)));
     __nv_bfloat162 out;
     memcpy(&out, &d, 4);
     return out;
