@@ -19,20 +19,29 @@ populations per step) are larger than L2, so no L2 flush is needed.
           overlaps the next frame's steps; the last copy is waited for inside
           the timed region.  e2e.blocking_readback: the same loop with the
           blocking lbm_read_moments; e2e.rendered_frames: reading back the
-          finished RGBA8 frame of lbm_render (render.rs's colour map).
-  fp16    the same lattice with half-precision deviation storage.
+          finished RGBA8 frame of lbm_render_async (render.rs's colour map).
+  fp16    the same lattice with half-precision deviation storage: the default
+          stochastic rounding, and round_nearest (LBM_ROUND_NEAREST).
   accuracy  rho/u L2 errors of the f32/f16/bf16 runs against the f64 run of
-          the same kernel after the same W + K steps.
+          the same kernel after the same W + K steps, and the same on the
+          laminar 1024^2 Taylor-Green vortex (taylor_green_1024).
+  taylor_green_256  the 256^2 periodic Taylor-Green lattice (tau 0.8, 1000
+          steps; L2-resident): GPU MLUPS in both arithmetics and both CPU
+          steppers on the host cores.
   roofline  algorithmic bytes (9 loads + 9 stores of 4 B + 1 B solid mask =
           73 B per cell) / average step time against the measured HBM copy
           bandwidth.
   batch   512 uneven lattices (sides U[64, 1024]) stepped together, autotuned.
-  large   16384^2 with 16-bit deviation storage against 8192^2 f32, and their
-          rho/u L2 errors against f64 on a 1024^2 window.
+  large   16384^2 with 16-bit deviation storage (both roundings) against
+          8192^2 f32, and their rho/u L2 errors against f64 on a 1024^2 window.
   learned the coarse-grid correction: 2048^2 fine vs 512^2 coarse channel,
           training on the GPU, velocity L2 of coarse-only and corrected runs
           against the fine run, time-to-solution ratio, and the network's
           forward throughput on the tensor cores.
+
+  cpu_baseline  the oracle's op-by-op CPU stepper (and the fused one) on all
+          host cores, 3 steps of the full lattice.
+  clocks  SM clock samples (nvidia-smi) during the timed region.
 
 --impl reference times the CPU implementation of the same step, restated op
 by op the way lbm.rs drives ArrayFire (oracle/, the reference cannot be built
