@@ -2,7 +2,8 @@
 //
 // No reference counterpart: a learned correction for a 4x-coarsened lattice.
 // The network is 4 layers of 3x3 convolutions, channels 4 -> 32 -> 32 -> 32
-// -> 9, GELU between layers, bf16 weights and activations, f32 accumulation.
+// -> 9, GELU (tanh form) between layers, bf16 weights and activations, f32
+// accumulation.
 //
 // Activation layout ("CB8"): [image][row + 1][channel block][x + 1][8] bf16,
 // i.e. blocks of 8 channels, a one-pixel zero halo around the image.  A run of
@@ -41,13 +42,25 @@ constexpr char kCnnMagic[8] = {'L', 'B', 'M', 'C', 'N', 'N', '0', '1'};
 __host__ __device__ constexpr int pad16(int c) { return (c + 15) / 16 * 16; }
 
 // GELU (erf form) and its derivative.
+// GELU in its tanh form, 0.5 x (1 + tanh(sqrt(2/pi) (x + 0.044715 x^3)))
+// (Hendrycks & Gimpel), with the hardware tanh.approx: a few FMAs and one
+// MUFU op per value, where the erf form costs tens of instructions and made
+// the convolution epilogue issue-bound.
+__device__ __forceinline__ float tanh_fast(float x) {
+    float y;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+constexpr float kGeluK = 0.7978845608028654f;     // sqrt(2 / pi)
+constexpr float kGeluC = 0.044715f;
 __device__ __forceinline__ float gelu(float x) {
-    return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f));
+    const float t = tanh_fast(kGeluK * fmaf(kGeluC * x, x * x, x));
+    return 0.5f * x * (1.0f + t);
 }
 __device__ __forceinline__ float gelu_grad(float x) {
-    const float cdf = 0.5f * (1.0f + erff(x * 0.70710678118654752f));
-    const float pdf = 0.39894228040143268f * expf(-0.5f * x * x);
-    return cdf + x * pdf;
+    const float t = tanh_fast(kGeluK * fmaf(kGeluC * x, x * x, x));
+    const float du = kGeluK * fmaf(3.0f * kGeluC, x * x, 1.0f);
+    return 0.5f * (1.0f + t) + 0.5f * x * (1.0f - t * t) * du;
 }
 
 struct ConvArgs {
@@ -165,7 +178,7 @@ conv3x3_tc_kernel(const ConvArgs a) {
                     g[c] = gelu(z[c]);
                 }
                 const int64_t o = cb8_chunk(b, y, cb, x, H, W, NO / 8);
-                reinterpret_cast<uint4*>(a.z_out)[o] = pack8_bf16(z);
+                if (a.z_out != nullptr) reinterpret_cast<uint4*>(a.z_out)[o] = pack8_bf16(z);
                 reinterpret_cast<uint4*>(a.x_out)[o] = pack8_bf16(g);
             }
         } else if constexpr (MODE == 1) {
@@ -461,7 +474,9 @@ int repack(lbm_cnn* N) {
 }
 
 // Forward pass over B images whose features are in N->x[0].
-int forward_impl(lbm_cnn* N, int B) {
+// Pre-activations are stored only for training (the backward pass needs
+// them); inference skips those writes.
+int forward_impl(lbm_cnn* N, int B, bool keep_z) {
     for (int l = 0; l < kLayers; ++l) {
         ConvArgs a{};
         a.in = N->x[l];
@@ -473,7 +488,7 @@ int forward_impl(lbm_cnn* N, int B) {
         a.err = N->err;
         cudaError_t e;
         if (l < kLayers - 1) {
-            a.z_out = N->z[l];
+            a.z_out = keep_z ? N->z[l] : nullptr;
             a.x_out = N->x[l + 1];
             e = (l == 0) ? launch_conv<2, 32, 0>(N, a) : launch_conv<4, 32, 0>(N, a);
         } else {
@@ -668,7 +683,7 @@ int lbm_cnn_forward(lbm_cnn* N, const float* in_dev, int batch, float* out_dev) 
     nchw_to_cb8_kernel<<<grid_of(int64_t(batch) * N->H * N->W * 2, 256), 256, 0, N->stream>>>(
         in_dev, batch, 4, N->H, N->W, 2, N->x[0]);
     CNN_CUDA(cudaGetLastError());
-    if (int rc = forward_impl(N, batch)) return rc;
+    if (int rc = forward_impl(N, batch, false)) return rc;
     CNN_CUDA(cudaMemcpyAsync(out_dev, N->out, size_t(batch) * 9 * N->H * N->W * 4,
                              cudaMemcpyDeviceToDevice, N->stream));
     return check_err(N);
@@ -681,7 +696,7 @@ int lbm_cnn_gradients(lbm_cnn* N, const float* in_dev, const float* target_dev, 
     nchw_to_cb8_kernel<<<grid_of(int64_t(batch) * N->H * N->W * 2, 256), 256, 0, N->stream>>>(
         in_dev, batch, 4, N->H, N->W, 2, N->x[0]);
     CNN_CUDA(cudaGetLastError());
-    if (int rc = forward_impl(N, batch)) return rc;
+    if (int rc = forward_impl(N, batch, true)) return rc;
     const double count = double(batch) * 9 * N->H * N->W;
     mse_kernel<<<1024, 256, 0, N->stream>>>(N->out, target_dev, batch, 9, N->H, N->W,
                                             float(2.0 / count), N->gbuf[kLayers], N->loss_partial);
@@ -776,7 +791,7 @@ int lbm_coarse_run(lbm_lattice* lat, lbm_cnn* N, int nsteps, int k, float s_rho,
         nchw_to_cb8_kernel<<<grid_of(int64_t(N->H) * N->W * 2, 256), 256, 0, N->stream>>>(
             N->feat, 1, 4, N->H, N->W, 2, N->x[0]);
         if (cudaGetLastError() != cudaSuccess) return finish(cfail(LBM_ERR_CUDA, "features launch"));
-        if (int rc = forward_impl(N, 1)) return finish(rc);
+        if (int rc = forward_impl(N, 1, false)) return finish(rc);
         if (int rc = lbm_coarse_apply(lat, N->out, 0, scale, max_abs)) return finish(rc);
         ++corrections;
         if (check_every > 0 && corrections % check_every == 0) {

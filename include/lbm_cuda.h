@@ -288,7 +288,7 @@ int lbm_render_async(lbm_lattice* lat, int mode, int geometry_overlay, uint8_t* 
 
 /* ---- learned coarse-grid correction --------------------------------------
  * No reference counterpart.  A 4-layer 3x3 convolutional network (channels
- * 4 -> 32 -> 32 -> 32 -> 9, GELU, bf16 weights, f32 accumulation on the
+ * 4 -> 32 -> 32 -> 32 -> 9, GELU (tanh form), bf16 weights, f32 accumulation on the
  * tensor cores) maps a coarse lattice's fields to a correction of its 9
  * populations.  Tensors passed as float* are device pointers in NCHW f32:
  * inputs (batch, 4, h, w) = ((rho - 1) * s_rho, ux * s_u, uy * s_u, solid);

@@ -2,7 +2,7 @@
 
 numpy restatement of the network liblbm_cuda.so trains on the tensor cores
 (4 layers of 3x3 'same' convolutions with zero padding, channels
-4 -> 32 -> 32 -> 32 -> 9, erf-GELU between layers, MSE loss), used by the
+4 -> 32 -> 32 -> 32 -> 9, GELU in its tanh form between layers, MSE loss), used by the
 tests as the checker of the GPU forward pass and gradients.  With bf16=True
 it rounds where the GPU stores bf16: weights, every layer input, the stored
 pre-activations and the loss gradient; sums are exact (f64).  With
@@ -15,7 +15,6 @@ W[tap = ky*3 + kx][cin][cout], then the biases[cout].
 from __future__ import annotations
 
 import numpy as np
-from scipy.special import erf
 
 CIN = (4, 32, 32, 32)
 COUT = (32, 32, 32, 9)
@@ -29,12 +28,18 @@ def bf16(x):
     return r.view(np.float32).astype(np.float64)
 
 
+K_GELU = np.sqrt(2.0 / np.pi)
+C_GELU = 0.044715
+
+
 def gelu(x):
-    return 0.5 * x * (1.0 + erf(x / np.sqrt(2.0)))
+    """GELU, tanh form: 0.5 x (1 + tanh(sqrt(2/pi) (x + 0.044715 x^3)))."""
+    return 0.5 * x * (1.0 + np.tanh(K_GELU * (x + C_GELU * x ** 3)))
 
 
 def gelu_grad(x):
-    return 0.5 * (1.0 + erf(x / np.sqrt(2.0))) + x * np.exp(-0.5 * x * x) / np.sqrt(2.0 * np.pi)
+    t = np.tanh(K_GELU * (x + C_GELU * x ** 3))
+    return 0.5 * (1.0 + t) + 0.5 * x * (1.0 - t * t) * K_GELU * (1.0 + 3.0 * C_GELU * x * x)
 
 
 def unpack(params):
