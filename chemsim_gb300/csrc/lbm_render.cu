@@ -53,18 +53,19 @@ __device__ __forceinline__ float field_value(const RenderField& f, int64_t o) {
     }
 }
 
-// Block partial sums of x (pass 0) or (x - mean)^2 (pass 1), in f64.
+// Block partial sums of x (pass 0) or (x - mean)^2 (pass 1), in f64.  Block
+// b takes rows b, b + grid, ...; its threads stride along the row.
 __global__ void __launch_bounds__(kRenderThreads)
 render_stats_kernel(RenderField f, int pass, const double* __restrict__ mean,
                     double* __restrict__ partial) {
-    const int64_t n = int64_t(f.w) * f.h;
     const double m = pass ? *mean : 0.0;
     double acc = 0.0;
-    for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < n;
-         e += int64_t(gridDim.x) * blockDim.x) {
-        const int y = int(e / f.w), x = int(e - int64_t(y) * f.w);
-        const double v = field_value(f, int64_t(y) * f.pitch + x);
-        acc += pass ? (v - m) * (v - m) : v;
+    for (int y = blockIdx.x; y < f.h; y += gridDim.x) {
+        const int64_t row = int64_t(y) * f.pitch;
+        for (int x = threadIdx.x; x < f.w; x += blockDim.x) {
+            const double v = field_value(f, row + x);
+            acc += pass ? (v - m) * (v - m) : v;
+        }
     }
     __shared__ double s[kRenderThreads];
     s[threadIdx.x] = acc;
@@ -76,14 +77,19 @@ render_stats_kernel(RenderField f, int pass, const double* __restrict__ mean,
     if (threadIdx.x == 0) partial[blockIdx.x] = s[0];
 }
 
-// stats[pass] = sum of the partials / n (fixed order); pass 1 stores the
-// standard deviation.
-__global__ void render_final_kernel(const double* __restrict__ partial, int64_t n, int pass,
-                                    double* __restrict__ stats) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    double s = 0.0;
-    for (int b = 0; b < kRenderBlocks; ++b) s += partial[b];
-    stats[pass] = pass ? sqrt(s / double(n)) : s / double(n);
+// stats[pass] = sum of the partials / n, a fixed-order tree over one block;
+// pass 1 stores the standard deviation.
+__global__ void __launch_bounds__(kRenderBlocks)
+render_final_kernel(const double* __restrict__ partial, int64_t n, int pass,
+                    double* __restrict__ stats) {
+    __shared__ double s[kRenderBlocks];
+    s[threadIdx.x] = partial[threadIdx.x];
+    __syncthreads();
+    for (int k = kRenderBlocks / 2; k > 0; k >>= 1) {
+        if (threadIdx.x < k) s[threadIdx.x] += s[threadIdx.x + k];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) stats[pass] = pass ? sqrt(s[0] / double(n)) : s[0] / double(n);
 }
 
 // HSV -> RGB, hexcone model: sector i = floor(6h), fraction f = 6h - i.
@@ -120,16 +126,15 @@ __device__ __forceinline__ float clamp01(float x) { return x != x ? x : fminf(fm
 __global__ void __launch_bounds__(kRenderThreads)
 render_pixels_kernel(RenderField f, const double* __restrict__ stats,
                      const uint8_t* __restrict__ solid, int mpitch, uchar4* __restrict__ out) {
-    const int64_t n = int64_t(f.w) * f.h;
     const float avg = float(stats[0]);
     const float inv_std = __fdiv_rn(1.f, float(stats[1]));
     const bool vec = f.mode == LBM_RENDER_VELOCITY || f.mode == LBM_RENDER_MOMENTUM;
     const float kPi = 3.14159265358979323846f;
     const float kHalfOverPi = __fmul_rn(0.318309886183790671538f, 0.5f);   // FRAC_1_PI * 0.5
-    for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < n;
-         e += int64_t(gridDim.x) * blockDim.x) {
-        const int y = int(e / f.w), x = int(e - int64_t(y) * f.w);
+    for (int y = blockIdx.x; y < f.h; y += gridDim.x)
+    for (int x = threadIdx.x; x < f.w; x += blockDim.x) {
         const int64_t o = int64_t(y) * f.pitch + x;
+        const int64_t e = int64_t(y) * f.w + x;
         uchar4 px;
         if (solid != nullptr && solid[int64_t(y) * mpitch + x]) {
             px = make_uchar4(0, 0, 255, 255);
@@ -191,10 +196,10 @@ int render_launch(lbm_lattice* L, int mode, int geometry_overlay, uchar4* dev_ou
     const int64_t n = int64_t(L->w) * L->h;
     for (int pass = 0; pass < 2; ++pass) {
         render_stats_kernel<<<kRenderBlocks, kRenderThreads, 0, L->stream>>>(f, pass, stats, partial);
-        render_final_kernel<<<1, 32, 0, L->stream>>>(partial, n, pass, stats);
+        render_final_kernel<<<1, kRenderBlocks, 0, L->stream>>>(partial, n, pass, stats);
     }
-    const int64_t blocks = std::min<int64_t>((n + kRenderThreads - 1) / kRenderThreads, 65535 * 8);
-    render_pixels_kernel<<<int(blocks), kRenderThreads, 0, L->stream>>>(
+    const int blocks = std::min(L->h, 65535 * 8);     // block b takes rows b, b + grid, ...
+    render_pixels_kernel<<<blocks, kRenderThreads, 0, L->stream>>>(
         f, stats, (geometry_overlay && L->has_solid) ? L->solid : nullptr, L->mpitch, out);
     if (img_out) *img_out = out;
     return cuda_status(cudaGetLastError(), "render launch");
