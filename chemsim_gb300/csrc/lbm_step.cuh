@@ -447,7 +447,7 @@ __device__ __forceinline__ void store_cells(const StepArgs<typename Store<S>::CT
 // Interior warp tile (flag 0): every source cell is inside the lattice and
 // fluid, so a step is 9 vector loads, 6 shuffles and two edge scalars per
 // lane, the collision and 9 vector stores.
-template <class S, int V, int FRAME, bool FAST>
+template <class S, int V, int FRAME, bool FAST, bool SR = false>
 __device__ __forceinline__ void step_interior(const StepArgs<typename Store<S>::CT>& a, int y,
                                               int x0, int lane) {
     using CT = typename Store<S>::CT;
@@ -488,7 +488,7 @@ __device__ __forceinline__ void step_interior(const StepArgs<typename Store<S>::
     collide_cells<S, V, FAST>(a.c, f);
     S enc[9][V];
 #pragma unroll
-    for (int i = 0; i < 9; ++i) ST::enc_vec_dom(f[i], enc[i], a.c.stochastic);
+    for (int i = 0; i < 9; ++i) ST::enc_vec_dom(f[i], enc[i], SR ? 1 : 0);
     store_cells<S, V, FAST>(a, y, x0, enc);
 }
 
@@ -505,7 +505,7 @@ __device__ __forceinline__ void step_interior(const StepArgs<typename Store<S>::
 // columns wrap.  On a partial last tile, lanes past the edge only feed the
 // shuffles, and the lane holding column w - 1 takes column 0 for the cell
 // whose source lies past the edge.
-template <class S, int V, int FRAME, bool FAST>
+template <class S, int V, int FRAME, bool FAST, bool SR = false>
 __device__ __forceinline__ void step_interior_wrap(const StepArgs<typename Store<S>::CT>& a, int y,
                                               int x0, int lane) {
     using CT = typename Store<S>::CT;
@@ -560,7 +560,7 @@ __device__ __forceinline__ void step_interior_wrap(const StepArgs<typename Store
     collide_cells<S, V, FAST>(a.c, f);
     S enc[9][V];
 #pragma unroll
-    for (int i = 0; i < 9; ++i) ST::enc_vec_dom(f[i], enc[i], a.c.stochastic);
+    for (int i = 0; i < 9; ++i) ST::enc_vec_dom(f[i], enc[i], SR ? 1 : 0);
     if (x0 < w) store_cells<S, V, FAST>(a, y, x0, enc);
 }
 
@@ -571,7 +571,7 @@ __device__ __forceinline__ void step_interior_wrap(const StepArgs<typename Store
 // classifies boundary links; phase C fetches the cell's own opposite
 // populations for bounce-back links (only near walls and solids); phase D
 // collides and stores.
-template <class S, int V, int FRAME, bool FAST>
+template <class S, int V, int FRAME, bool FAST, bool SR = false>
 __device__ __forceinline__ void step_general(const StepArgs<typename Store<S>::CT>& a, int y,
                                              int tile, int lane) {
     using CT = typename Store<S>::CT;
@@ -740,7 +740,7 @@ __device__ __forceinline__ void step_general(const StepArgs<typename Store<S>::C
     S enc[9][V];
     collide_cells<S, V, FAST>(a.c, f);
 #pragma unroll
-    for (int i = 0; i < 9; ++i) ST::enc_vec_dom(f[i], enc[i], a.c.stochastic);
+    for (int i = 0; i < 9; ++i) ST::enc_vec_dom(f[i], enc[i], SR ? 1 : 0);
 
     if (own_solid && halfway) {
         // Half-way mode: solid nodes keep their populations.
@@ -771,7 +771,7 @@ __device__ __forceinline__ void step_general(const StepArgs<typename Store<S>::C
 #ifndef LBM_STEP_MIN_BLOCKS_16
 #define LBM_STEP_MIN_BLOCKS_16 3
 #endif
-template <class S, int V, int FRAME, bool FAST>
+template <class S, int V, int FRAME, bool FAST, bool SR>
 __global__ void __launch_bounds__(256, (sizeof(typename Store<S>::CT) == 4 && V <= 4)
                                            ? (sizeof(S) == 2 ? LBM_STEP_MIN_BLOCKS_16 : LBM_STEP_MIN_BLOCKS)
                                            : 1)
@@ -784,7 +784,7 @@ lbm_step_kernel(const StepArgs<typename Store<S>::CT> a) {
         if (e >= a.ngtiles) return;
         const uint32_t t = a.gtiles[e];
         const int y = int(t / uint32_t(a.ntiles));
-        step_general<S, V, FRAME, FAST>(a, y, int(t - uint32_t(y) * uint32_t(a.ntiles)), threadIdx.x);
+        step_general<S, V, FRAME, FAST, SR>(a, y, int(t - uint32_t(y) * uint32_t(a.ntiles)), threadIdx.x);
         return;
     }
     const int ib = b - gblocks;
@@ -792,23 +792,23 @@ lbm_step_kernel(const StepArgs<typename Store<S>::CT> a) {
     const int y = by * rows + threadIdx.y;
     if (y >= a.h) return;                                                  // warp-uniform
     if (a.tflags == nullptr) {
-        step_general<S, V, FRAME, FAST>(a, y, tile, threadIdx.x);
+        step_general<S, V, FRAME, FAST, SR>(a, y, tile, threadIdx.x);
         return;
     }
     const uint8_t flag = a.tflags[int64_t(y) * a.ntiles + tile];        // warp-uniform
     if (flag == 1) return;                                                 // owned by the list
-    if (flag == 0) step_interior<S, V, FRAME, FAST>(a, y, (tile * 32 + threadIdx.x) * V, threadIdx.x);
-    else step_interior_wrap<S, V, FRAME, FAST>(a, y, (tile * 32 + threadIdx.x) * V, threadIdx.x);
+    if (flag == 0) step_interior<S, V, FRAME, FAST, SR>(a, y, (tile * 32 + threadIdx.x) * V, threadIdx.x);
+    else step_interior_wrap<S, V, FRAME, FAST, SR>(a, y, (tile * 32 + threadIdx.x) * V, threadIdx.x);
 }
 
-template <class S, int V, int FRAME, bool FAST>
+template <class S, int V, int FRAME, bool FAST, bool SR>
 void launch_step_tv(const StepArgs<typename Store<S>::CT>& a, int rows, cudaStream_t stream) {
     const int ntiles = (a.w + 32 * V - 1) / (32 * V);
     const int rowblocks = (a.h + rows - 1) / rows;
     const int gblocks = a.tflags != nullptr ? (a.ngtiles + rows - 1) / rows : 0;
     StepArgs<typename Store<S>::CT> b = a;
     b.ntiles = ntiles;
-    lbm_step_kernel<S, V, FRAME, FAST><<<gblocks + ntiles * rowblocks, dim3(32, rows), 0, stream>>>(b);
+    lbm_step_kernel<S, V, FRAME, FAST, SR><<<gblocks + ntiles * rowblocks, dim3(32, rows), 0, stream>>>(b);
 }
 
 // One step: the interior kernel plus the general kernel over the flagged
@@ -817,12 +817,26 @@ template <class S, int V>
 cudaError_t launch_step_v(const StepArgs<typename Store<S>::CT>& a, int frame, bool fast,
                           int rows, cudaStream_t stream) {
     (void)cudaGetLastError();   // report this launch's status, not an earlier call's
+    // 16-bit storage: the rounding of the stores is a compile-time choice
+    // (a runtime choice between the two conversions cost about 4%)
+    if constexpr (Store<S>::DEV) {
+        if (a.c.stochastic) {
+            if (frame) {
+                if (fast) launch_step_tv<S, V, 1, true, true>(a, rows, stream);
+                else launch_step_tv<S, V, 1, false, true>(a, rows, stream);
+            } else {
+                if (fast) launch_step_tv<S, V, 0, true, true>(a, rows, stream);
+                else launch_step_tv<S, V, 0, false, true>(a, rows, stream);
+            }
+            return cudaGetLastError();
+        }
+    }
     if (frame) {
-        if (fast) launch_step_tv<S, V, 1, true>(a, rows, stream);
-        else launch_step_tv<S, V, 1, false>(a, rows, stream);
+        if (fast) launch_step_tv<S, V, 1, true, false>(a, rows, stream);
+        else launch_step_tv<S, V, 1, false, false>(a, rows, stream);
     } else {
-        if (fast) launch_step_tv<S, V, 0, true>(a, rows, stream);
-        else launch_step_tv<S, V, 0, false>(a, rows, stream);
+        if (fast) launch_step_tv<S, V, 0, true, false>(a, rows, stream);
+        else launch_step_tv<S, V, 0, false, false>(a, rows, stream);
     }
     return cudaGetLastError();
 }
