@@ -129,6 +129,7 @@ SIGNATURES = {
     "lbm_cnn_gradients": (_i32, [_vp, _vp, _vp, _i32, ctypes.POINTER(_f32), _vp]),
     "lbm_cnn_train_step": (_i32, [_vp, _vp, _vp, _i32, _f32, ctypes.POINTER(_f32)]),
     "lbm_cnn_set_stream": (_i32, [_vp, _vp]),
+    "lbm_selftest_wait_timeout": (_i32, [ctypes.c_uint32, ctypes.POINTER(_i32)]),
     "lbm_cnn_save": (_i32, [_vp, ctypes.c_char_p]),
     "lbm_cnn_load": (_i32, [_vp, ctypes.c_char_p]),
     "lbm_coarse_run": (_i32, [_vp, _vp, _i32, _i32, _f32, _f32, _f32, _f32, _i32, _f32,

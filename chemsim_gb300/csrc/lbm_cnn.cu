@@ -387,6 +387,16 @@ __global__ void adam_kernel(float* __restrict__ p, const float* __restrict__ g, 
     }
 }
 
+// One warp waits on an mbarrier that nothing signals, with the same bounded
+// wait as the convolution kernels, and records that it gave up.
+__global__ void wait_probe_kernel(int* __restrict__ timed_out, uint32_t polls) {
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) lbmtc::mbar_init(&bar, 1);
+    __syncthreads();
+    const bool ok = lbmtc::mbar_wait_bounded(&bar, 0, polls);
+    if (!ok && threadIdx.x == 0) atomicExch(timed_out, 1);
+}
+
 int grid_of(int64_t n, int block) {
     int64_t g = (n + block - 1) / block;
     if (g > 65535 * 4) g = 65535 * 4;
@@ -727,6 +737,23 @@ int lbm_cnn_train_step(lbm_cnn* N, const float* in_dev, const float* target_dev,
                                                                   1e-8f, c1, c2);
     CNN_CUDA(cudaGetLastError());
     if (int rc = repack(N)) return rc;
+    return LBM_OK;
+}
+
+int lbm_selftest_wait_timeout(uint32_t polls, int* timed_out) {
+    if (!timed_out) return cfail(LBM_ERR_INVALID_ARGUMENT, "null argument");
+    if (polls < 1 || polls > kWaitPolls) return cfail(LBM_ERR_INVALID_ARGUMENT, "polls out of range");
+    *timed_out = 0;
+    int* d = nullptr;
+    CNN_CUDA(cudaMalloc(&d, sizeof(int)));
+    cudaError_t e = cudaMemset(d, 0, sizeof(int));
+    if (e == cudaSuccess) {
+        wait_probe_kernel<<<1, 32>>>(d, polls);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(timed_out, d, sizeof(int), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    CNN_CUDA(e);
     return LBM_OK;
 }
 

@@ -122,7 +122,7 @@ def coarse_run(lat, net, nsteps: int, k: int, s_rho: float, s_u: float, scale: f
 # the coarse-plus-correction experiment
 # ---------------------------------------------------------------------------
 
-from dataclasses import dataclass, field  # noqa: E402
+from dataclasses import dataclass  # noqa: E402
 import time  # noqa: E402
 
 
@@ -159,7 +159,6 @@ class CorrectionConfig:
     data_policy: str = "teacher"  # first data pass: "teacher" or "none" (coarse-only run)
     onpolicy_passes: int = 0      # data passes with the network's own corrections applied
     onpolicy_iters: int = 1500
-    extra: dict = field(default_factory=dict)
 
     @property
     def coarse(self) -> int:
@@ -425,7 +424,7 @@ def run_correction_experiment(cfg: CorrectionConfig, log=None, gains=None) -> di
     geometry (evaluate_correction).  Returns a result dict."""
     import torch
     stream = torch.cuda.Stream()
-    res = {"config": {k: v for k, v in cfg.__dict__.items() if k != "extra"},
+    res = {"config": dict(cfg.__dict__),
            "tau_coarse": cfg.tau_coarse, "force_coarse": cfg.force_fine * cfg.factor}
     net, s_eff, res["training"] = train_correction(cfg, stream, log)
     res["training"]["target_rms"] = s_eff

@@ -313,6 +313,12 @@ int lbm_cnn_gradients(lbm_cnn* net, const float* in, const float* target, int ba
 /* One Adam step (beta1 0.9, beta2 0.999) on the MSE loss.                  */
 int lbm_cnn_train_step(lbm_cnn* net, const float* in, const float* target, int batch,
                        float lr, float* loss);
+/* Diagnostic of the bounded device waits: one warp waits on an mbarrier that
+ * nothing signals, giving up after `polls` polls (1 .. 4194304; each poll
+ * sleeps about 32 ns) through the same routine the tensor-core kernels use,
+ * and *timed_out reports that it gave up.  The context stays usable: this is
+ * the path a lost arrival takes (those kernels then return LBM_ERR_TIMEOUT). */
+int lbm_selftest_wait_timeout(uint32_t polls, int* timed_out);
 /* Weights to / from a file: "LBMCNN01", int64 parameter count, the f32
  * parameters in lbm_cnn_get_params order.                                  */
 int lbm_cnn_save(lbm_cnn* net, const char* path);

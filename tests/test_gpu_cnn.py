@@ -219,3 +219,18 @@ def test_learned_correction_beats_coarse_only(gpu):
     print({"coarse_only": ev["u_l2_coarse_only"], "corrected": corr["u_l2"]})
     assert corr["fallback_triggered_at_fine_step"] is None
     assert all(c < b for c, b in zip(corr["u_l2"], ev["u_l2_coarse_only"]))
+
+
+def test_bounded_wait_times_out_and_context_survives(gpu):
+    """A wait on an mbarrier that nothing signals gives up after its poll
+    limit and reports it; the device keeps working afterwards."""
+    import ctypes
+    lib = lbm._lib.load()
+    out = ctypes.c_int(0)
+    lbm._lib.check(lib.lbm_selftest_wait_timeout(1000, ctypes.byref(out)))
+    assert out.value == 1
+    with pytest.raises(lbm.LBMError):
+        lbm._lib.check(lib.lbm_selftest_wait_timeout(0, ctypes.byref(out)))
+    with Lattice(64, 32, 0.8, F32, X_PERIODIC | Y_WALL | FRAME_XY) as lat:
+        lat.step(5)
+        assert not lat.health()["unstable"]
