@@ -385,7 +385,7 @@ def run_ours(args):
                 "traffic_unit": "GB per launch"}
     fp16 = {"mlups": round(mlups16, 1), "speedup_vs_f32": round(mlups16 / mlups32, 3),
             "achieved_gbs": round((BYTES_F16 + BYTES_MASK) * cells / (t16 / args.steps) / 1e9, 1),
-            "rounding": "stochastic (hashed from the value's bits)",
+            "rounding": "stochastic (random bits from the pair's own f32 bits)",
             "round_nearest": {"mlups": round(mlups16n, 1),
                               "speedup_vs_f32": round(mlups16n / mlups32, 3)}}
 

@@ -65,7 +65,8 @@ size_t elem_size(int precision) {
 int default_cells(int precision) {
     switch (precision) {
         case LBM_F64: return 2;
-        default: return 4;
+        case LBM_F32: return 4;
+        default: return 8;      // 16-bit: one 16-byte load per plane and thread
     }
 }
 
@@ -379,6 +380,7 @@ StepArgs<typename Store<S>::CT> lattice_args(const lbm_lattice* L, int from, boo
     if (moments) { a.mom_rho = L->mom[0]; a.mom_ux = L->mom[1]; a.mom_uy = L->mom[2]; }
     a.w = L->w; a.h = L->h; a.pitch = L->pitch; a.mpitch = L->mpitch; a.plane = L->plane;
     a.flags = L->flags;
+    a.pf_rows = -1;          // the launcher sizes the L2 prefetch distance
     a.c = make_consts<CT>(L);
     return a;
 }

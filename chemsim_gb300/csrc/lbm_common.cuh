@@ -149,10 +149,13 @@ template <> __device__ inline float DevStore<__nv_bfloat16, __nv_bfloat162>::to_
 template <> __device__ inline __nv_bfloat16 DevStore<__nv_bfloat16, __nv_bfloat162>::from_f(float f) { return __float2bfloat16_rn(f); }
 template <> __device__ inline float2 DevStore<__nv_bfloat16, __nv_bfloat162>::to_f2(__nv_bfloat162 s) { return __bfloat1622float2(s); }
 template <> __device__ inline __nv_bfloat162 DevStore<__nv_bfloat16, __nv_bfloat162>::from_f2(float2 f) { return __float22bfloat162_rn(f); }
-// Random bits of a pair for the stochastic-rounding conversion: multiplicative
-// hashes of both values' f32 bits, so a run is reproducible bit for bit.
+// Random bits of a pair for the stochastic-rounding conversion: one
+// multiply-add of both values' f32 bits (the low bits that a conversion
+// drops are noise-like, and the multiply spreads each value's bits upward),
+// so a run is reproducible bit for bit.  Two multiplies and an xor measured
+// no more accurate and 3-4% slower.
 __device__ __forceinline__ uint32_t sr_bits(float lo, float hi) {
-    return (__float_as_uint(lo) * 0x9E3779B1u) ^ (__float_as_uint(hi) * 0x85EBCA77u);
+    return __float_as_uint(lo) * 0x9E3779B1u + __float_as_uint(hi);
 }
 // cvt.rs: the hardware stochastic-rounding conversion of sm_100-class GPUs.
 template <>
@@ -218,6 +221,7 @@ struct StepArgs {
     int w, h, pitch, mpitch;
     int64_t plane;          // plane stride in elements
     int flags;
+    int pf_rows;            // L2 prefetch distance in rows: 0 off, < 0 chosen at launch
     Consts<CT> c;
 };
 

@@ -444,6 +444,37 @@ __device__ __forceinline__ void store_cells(const StepArgs<typename Store<S>::CT
     }
 }
 
+// L2 prefetch ahead of the wavefront: blocks run in row-major order, so the
+// rows that the warp a.pf_rows rows further down will pull are fetched into
+// L2 now (one bulk prefetch of the warp's 32 V columns per plane, lanes 0-8)
+// and that warp's loads find them there.  Interior tiles only (full tiles, so
+// the range stays inside the row).
+template <class S, int V, int FRAME, class CT>
+__device__ __forceinline__ void prefetch_ahead(const StepArgs<CT>& a, int y, int x0, int lane) {
+    if (a.pf_rows > 0 && lane < 9) {
+        const int ys = y + a.pf_rows - DROW(FRAME, lane);
+        if (ys < a.h) {
+            const S* p = static_cast<const S*>(a.src) + lane * a.plane + int64_t(ys) * a.pitch +
+                         (x0 - lane * V);
+            asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;"
+                         :: "l"(p), "n"(32 * V * int(sizeof(S))) : "memory");
+        }
+    }
+}
+
+// 16-bit storage with stochastic rounding: the cells of a partial last chunk
+// that lie past the lattice edge collide zeros.  A stored cell's rounding
+// hashes its pair partner too, so the partner must not depend on which path
+// loaded it.
+template <class S, int V>
+__device__ __forceinline__ void zero_past_edge(typename Store<S>::CT (&f)[9][V], int x0, int w) {
+#pragma unroll
+    for (int i = 0; i < 9; ++i)
+#pragma unroll
+        for (int k = 0; k < V; ++k)
+            if (x0 + k >= w) f[i][k] = 0;
+}
+
 // Interior warp tile (flag 0): every source cell is inside the lattice and
 // fluid, so a step is 9 vector loads, 6 shuffles and two edge scalars per
 // lane, the collision and 9 vector stores.
@@ -465,6 +496,7 @@ __device__ __forceinline__ void step_interior(const StepArgs<typename Store<S>::
         if (dc == 1 && lane == 0) edge[i] = __ldg(p - 1);
         if (dc == -1 && lane == 31) edge[i] = __ldg(p + V);
     }
+    prefetch_ahead<S, V, FRAME>(a, y, x0, lane);
     CT f[9][V];
 #pragma unroll
     for (int i = 0; i < 9; ++i) {
@@ -528,7 +560,7 @@ __device__ __forceinline__ void step_interior_wrap(const StepArgs<typename Store
         if (dc == 1 && lane == 0) edge[i] = __ldg(prow + (x0 == 0 ? w - 1 : x0 - 1));
         if (dc == -1) {
             if (last) edge[i] = __ldg(prow);               // column w wraps to 0
-            else if (lane == 31) edge[i] = __ldg(prow + x0 + V);
+            else if (lane == 31 && x0 < w) edge[i] = __ldg(prow + x0 + V);
         }
     }
     CT f[9][V];
@@ -557,11 +589,224 @@ __device__ __forceinline__ void step_interior_wrap(const StepArgs<typename Store
 #pragma unroll
         for (int k = 0; k < V; ++k) f[i][k] = v[k];
     }
+    if (SR && last) zero_past_edge<S, V>(f, x0, w);
     collide_cells<S, V, FAST>(a.c, f);
     S enc[9][V];
 #pragma unroll
     for (int i = 0; i < 9; ++i) ST::enc_vec_dom(f[i], enc[i], SR ? 1 : 0);
     if (x0 < w) store_cells<S, V, FAST>(a, y, x0, enc);
+}
+
+// 16-bit storage keeps a thread's values packed two per register (element
+// 2j in the low half of register j) until the collision: the +-1 column
+// shifts become one byte permute per register, and only one cell pair is
+// widened to f32 at a time, so the working set stays small enough for V = 8.
+template <int NP>
+struct PackIO {
+    __device__ __forceinline__ static void load(const void* p, uint32_t (&r)[NP]) {
+        if constexpr (NP == 4) {
+            const uint4 q = __ldg(reinterpret_cast<const uint4*>(p));
+            r[0] = q.x; r[1] = q.y; r[2] = q.z; r[3] = q.w;
+        } else {
+            static_assert(NP == 2, "4 or 8 cells per thread");
+            const uint2 q = __ldg(reinterpret_cast<const uint2*>(p));
+            r[0] = q.x; r[1] = q.y;
+        }
+    }
+    __device__ __forceinline__ static void store(void* p, const uint32_t (&r)[NP]) {
+        if constexpr (NP == 4) *reinterpret_cast<uint4*>(p) = make_uint4(r[0], r[1], r[2], r[3]);
+        else *reinterpret_cast<uint2*>(p) = make_uint2(r[0], r[1]);
+    }
+};
+
+// Pull shift by one column toward higher x (c_x = +1 in the row direction):
+// element k takes element k - 1; `left` holds the value entering at k = 0 in
+// its high half.
+template <int NP>
+__device__ __forceinline__ void shift_up_packed(uint32_t (&r)[NP], uint32_t left) {
+#pragma unroll
+    for (int j = NP - 1; j > 0; --j) r[j] = __byte_perm(r[j - 1], r[j], 0x5432);
+    r[0] = __byte_perm(left, r[0], 0x5432);
+}
+// Element k takes element k + 1; `right` holds the value entering at the top
+// in its low half.
+template <int NP>
+__device__ __forceinline__ void shift_down_packed(uint32_t (&r)[NP], uint32_t right) {
+#pragma unroll
+    for (int j = 0; j < NP - 1; ++j) r[j] = __byte_perm(r[j], r[j + 1], 0x5432);
+    r[NP - 1] = __byte_perm(r[NP - 1], right, 0x5432);
+}
+// Replaces element k of a packed row by the 16-bit value e.
+template <int NP>
+__device__ __forceinline__ void set_packed(uint32_t (&r)[NP], int k, uint32_t e) {
+#pragma unroll
+    for (int j = 0; j < NP; ++j) {
+        if (k == 2 * j) r[j] = (r[j] & 0xffff0000u) | (e & 0xffffu);
+        else if (k == 2 * j + 1) r[j] = (r[j] & 0xffffu) | (e << 16);
+    }
+}
+
+// Collides the pairs of a packed 16-bit tile in place.  Every pair is
+// widened, collided by collide_dev_x2 and narrowed exactly as collide_cells +
+// enc_vec_dom do, so the results are the same bits as the unpacked path's.
+// With SUB (general tiles), zero-padded links (bit k of zb[i]) take the
+// deviation value of f = 0 after widening, and cells past the lattice edge
+// (bit k of past) collide zeros under stochastic rounding (zero_past_edge).
+template <class S, int V, bool SR, bool SUB = false>
+__device__ __forceinline__ void collide_packed(const Consts<float>& c, uint32_t (&r)[9][V / 2],
+                                               const uint32_t* zb = nullptr, uint32_t past = 0u) {
+    using ST = Store<S>;
+    using H2 = decltype(ST::from_f2(make_float2(0.f, 0.f)));
+    constexpr int NP = V / 2;
+    uint32_t any = SR ? past : 0u;                 // cells that take a substitute
+    if constexpr (SUB) {
+#pragma unroll
+        for (int i = 0; i < 9; ++i) any |= zb[i];
+    }
+#pragma unroll
+    for (int j = 0; j < NP; ++j) {
+        float2 g[9], o[9];
+#pragma unroll
+        for (int i = 0; i < 9; ++i) {
+            H2 p;
+            memcpy(&p, &r[i][j], 4);
+            g[i] = ST::to_f2(p);
+        }
+        if (SUB && ((any >> (2 * j)) & 3u)) {
+#pragma unroll
+            for (int i = 0; i < 9; ++i) {
+                const uint32_t z = zb[i] >> (2 * j);
+                const float zv = ST::zero_dom(c.wt[i], c.dscale);
+                if (z & 1u) g[i].x = zv;
+                if (z & 2u) g[i].y = zv;
+                if (SR && ((past >> (2 * j)) & 1u)) g[i].x = 0.f;
+                if (SR && ((past >> (2 * j)) & 2u)) g[i].y = 0.f;
+            }
+        }
+        collide_dev_x2(c, g, o);
+#pragma unroll
+        for (int i = 0; i < 9; ++i) {
+            const H2 p = SR ? ST::from_f2_sr(o[i].x, o[i].y) : ST::from_f2(o[i]);
+            memcpy(&r[i][j], &p, 4);
+        }
+    }
+}
+
+// Writes a packed tile's cells of row y from column x0 (and the moments when
+// requested).
+template <class S, int V>
+__device__ __forceinline__ void store_packed(const StepArgs<float>& a, int y, int x0,
+                                             const uint32_t (&r)[9][V / 2]) {
+    constexpr int NP = V / 2;
+    if (x0 + V <= a.w && a.mom_rho == nullptr) {
+        S* __restrict__ dst = static_cast<S*>(a.dst) + int64_t(y) * a.pitch + x0;
+#pragma unroll
+        for (int i = 0; i < 9; ++i) PackIO<NP>::store(dst + i * a.plane, r[i]);
+        return;
+    }
+    S enc[9][V];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) memcpy(enc[i], r[i], sizeof(enc[i]));
+    store_cells<S, V, true>(a, y, x0, enc);
+}
+
+template <class S, int V, bool SR>
+__device__ __forceinline__ void collide_store_packed(const StepArgs<float>& a, int y, int x0,
+                                                     uint32_t (&r)[9][V / 2]) {
+    collide_packed<S, V, SR>(a.c, r);
+    store_packed<S, V>(a, y, x0, r);
+}
+
+// Mask of the 16-bit halves of register j selected by bits 2j, 2j + 1 of b.
+__device__ __forceinline__ uint32_t half_mask(uint32_t b, int j) {
+    return (((b >> (2 * j)) & 1u) ? 0x0000ffffu : 0u) | (((b >> (2 * j + 1)) & 1u) ? 0xffff0000u : 0u);
+}
+
+// Interior warp tile (flag 0) of 16-bit storage, packed.
+template <class S, int V, int FRAME, bool SR>
+__device__ __forceinline__ void step_interior_packed(const StepArgs<float>& a, int y, int x0,
+                                                     int lane) {
+    constexpr int NP = V / 2;
+    const S* __restrict__ base = static_cast<const S*>(a.src) + int64_t(y) * a.pitch + x0;
+    const int64_t P = a.pitch, PL = a.plane;
+    uint32_t r[9][NP];
+    uint32_t edge[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+        const int dc = DCOL(FRAME, i), dr = DROW(FRAME, i);
+        const S* p = base + i * PL - dr * P;
+        PackIO<NP>::load(p, r[i]);
+        edge[i] = 0u;
+        if (dc == 1 && lane == 0) edge[i] = uint32_t(__ldg(reinterpret_cast<const unsigned short*>(p - 1))) << 16;
+        if (dc == -1 && lane == 31) edge[i] = __ldg(reinterpret_cast<const unsigned short*>(p + V));
+    }
+    prefetch_ahead<S, V, FRAME>(a, y, x0, lane);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+        const int dc = DCOL(FRAME, i);
+        if (dc == 1) {
+            const uint32_t left = __shfl_up_sync(kFull, r[i][NP - 1], 1);
+            shift_up_packed<NP>(r[i], lane == 0 ? edge[i] : left);
+        } else if (dc == -1) {
+            const uint32_t right = __shfl_down_sync(kFull, r[i][0], 1);
+            shift_down_packed<NP>(r[i], lane == 31 ? edge[i] : right);
+        }
+    }
+    collide_store_packed<S, V, SR>(a, y, x0, r);
+}
+
+// Periodic-edge warp tile (flag 2) of 16-bit storage, packed (the rules of
+// step_interior_wrap).
+template <class S, int V, int FRAME, bool SR>
+__device__ __forceinline__ void step_interior_wrap_packed(const StepArgs<float>& a, int y, int x0,
+                                                          int lane) {
+    constexpr int NP = V / 2;
+    const int w = a.w, h = a.h;
+    const int64_t P = a.pitch, PL = a.plane;
+    const S* __restrict__ src = static_cast<const S*>(a.src);
+    const int ym1 = y == 0 ? h - 1 : y - 1, yp1 = y == h - 1 ? 0 : y + 1;
+    const int xl = x0 < w ? x0 : 0;
+    const bool last = x0 < w && x0 + V >= w;
+    uint32_t r[9][NP];
+    uint32_t edge[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+        const int dc = DCOL(FRAME, i), dr = DROW(FRAME, i);
+        const int sr = dr == 1 ? ym1 : (dr == -1 ? yp1 : y);
+        const unsigned short* prow =
+            reinterpret_cast<const unsigned short*>(src + i * PL + int64_t(sr) * P);
+        PackIO<NP>::load(prow + xl, r[i]);
+        edge[i] = 0u;
+        if (dc == 1 && lane == 0) edge[i] = uint32_t(__ldg(prow + (x0 == 0 ? w - 1 : x0 - 1))) << 16;
+        if (dc == -1) {
+            if (last) edge[i] = __ldg(prow);                  // column w wraps to 0
+            else if (lane == 31 && x0 < w) edge[i] = __ldg(prow + x0 + V);
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+        const int dc = DCOL(FRAME, i);
+        if (dc == 1) {
+            const uint32_t left = __shfl_up_sync(kFull, r[i][NP - 1], 1);
+            shift_up_packed<NP>(r[i], lane == 0 ? edge[i] : left);
+        } else if (dc == -1) {
+            const uint32_t right = __shfl_down_sync(kFull, r[i][0], 1);
+            shift_down_packed<NP>(r[i], lane == 31 ? edge[i] : right);
+            if (last) set_packed<NP>(r[i], w - 1 - x0, edge[i]);
+        }
+    }
+    if (x0 >= w) return;                 // lanes past the edge only fed the shuffles
+    if (SR && x0 + V > w) {
+        // cells past the edge collide zeros: a stored cell's stochastic
+        // rounding hashes its pair partner too, which must not depend on
+        // the path that ran
+#pragma unroll
+        for (int i = 0; i < 9; ++i)
+#pragma unroll
+            for (int k = 0; k < V; ++k)
+                if (x0 + k >= w) set_packed<NP>(r[i], k, 0u);
+    }
+    collide_store_packed<S, V, SR>(a, y, x0, r);
 }
 
 // One time step of one lattice.  Phase A issues every global load of the
@@ -737,6 +982,7 @@ __device__ __forceinline__ void step_general(const StepArgs<typename Store<S>::C
     }
 
     // ---- phase D: collide and write ---------------------------------------
+    if (SR && x0 + V > w) zero_past_edge<S, V>(f, x0, w);
     S enc[9][V];
     collide_cells<S, V, FAST>(a.c, f);
 #pragma unroll
@@ -758,6 +1004,183 @@ __device__ __forceinline__ void step_general(const StepArgs<typename Store<S>::C
     store_cells<S, V, FAST>(a, y, x0, enc);
 }
 
+// General tile of 16-bit storage, packed: the rules of step_general with the
+// values kept two per register.  Bounce-back links, the solid swap and the
+// half-way keep move raw 16-bit values (exact in either form); zero-padded
+// links are substituted after widening, where the value f = 0 has its exact
+// f32 deviation form.
+template <class S, int V, int FRAME, bool SR>
+__device__ __forceinline__ void step_general_packed(const StepArgs<float>& a, int y, int tile,
+                                                    int lane) {
+    constexpr int NP = V / 2;
+    constexpr uint32_t FULL = (1u << V) - 1u;
+    const int w = a.w, h = a.h;
+    const int x0 = (tile * 32 + lane) * V;
+    const bool active = x0 < w;
+    const int xl = active ? x0 : 0;
+    const unsigned short* __restrict__ src = static_cast<const unsigned short*>(a.src);
+    const int64_t P = a.pitch, PL = a.plane;
+    const int xm = a.flags & 3, ym = (a.flags >> 2) & 3;
+    const bool halfway = (a.flags & LBM_SOLID_HALFWAY) != 0;
+    const bool has_solid = a.solid != nullptr;
+    const bool xper = xm == 1;
+    const bool left_edge = lane == 0 || x0 == 0;
+    const bool right_edge = lane == 31 || x0 + V >= w;
+
+    // ---- phase A: issue all loads ----------------------------------------
+    uint32_t mcore[3] = {0u, 0u, 0u}, mleft[3] = {0u, 0u, 0u}, mright[3] = {0u, 0u, 0u};
+    if (has_solid) {
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            int row = y - 1 + r;
+            bool ok = true;
+            if (row < 0 || row >= h) {
+                if (ym == 1) row = row < 0 ? row + h : row - h;
+                else ok = false;
+            }
+            if (ok) {
+                const uint8_t* mr = a.solid + int64_t(row) * a.mpitch;
+                mcore[r] = load_mask_core<V>(mr + xl);
+                if (left_edge) mleft[r] = mask_at(mr, x0 - 1, w, xper);
+                if (right_edge) mright[r] = mask_at(mr, x0 + V, w, xper);
+            }
+        }
+    }
+    uint32_t r[9][NP];
+    uint32_t edge[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+        const int dc = DCOL(FRAME, i), dr = DROW(FRAME, i);
+        int cls;
+        const int sr = source_row(y, dr, h, ym, &cls);
+        const unsigned short* prow = src + i * PL + int64_t(sr) * P;
+        PackIO<NP>::load(prow + xl, r[i]);
+        edge[i] = 0u;
+        if (dc == 1) {
+            int ec = x0 - 1;
+            if (ec < 0) ec = xper ? w - 1 : -1;
+            if (left_edge && ec >= 0) edge[i] = uint32_t(__ldg(prow + ec)) << 16;
+        } else if (dc == -1) {
+            int ec = x0 + V;
+            if (ec >= w) ec = (xper && ec == w) ? 0 : -1;
+            if (right_edge && ec >= 0) edge[i] = __ldg(prow + ec);
+        }
+    }
+
+    // ---- phase B: realign, classify ---------------------------------------
+    uint32_t mrow[3] = {0u, 0u, 0u};
+    if (has_solid) {
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            uint32_t core = mcore[q];
+            const uint32_t l = __shfl_up_sync(kFull, (core >> (V - 1)) & 1u, 1);
+            const uint32_t rr = __shfl_down_sync(kFull, core & 1u, 1);
+            if (x0 + V > w && xper) {
+                int row = y - 1 + q;
+                if (row < 0) row += h;
+                if (row >= h) row -= h;
+                const uint8_t* mr = a.solid + int64_t(row) * a.mpitch;
+#pragma unroll
+                for (int k = 0; k < V; ++k)
+                    if (x0 + k >= w) core = (core & ~(1u << k)) | (mask_at(mr, x0 + k, w, true) << k);
+            }
+            mrow[q] = (left_edge ? mleft[q] : l) | (core << 1) | ((right_edge ? mright[q] : rr) << (V + 1));
+        }
+    }
+    uint32_t zb[9], bnc[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+        const int dc = DCOL(FRAME, i), dr = DROW(FRAME, i);
+        uint32_t xz = 0u, xb = 0u;
+        if (dc == 1) {
+            const uint32_t left = __shfl_up_sync(kFull, r[i][NP - 1], 1);
+            shift_up_packed<NP>(r[i], left_edge ? edge[i] : left);
+            if (x0 == 0 && !xper) { if (xm == 2) xb |= 1u; else xz |= 1u; }
+        } else if (dc == -1) {
+            const uint32_t right = __shfl_down_sync(kFull, r[i][0], 1);
+            shift_down_packed<NP>(r[i], right_edge ? edge[i] : right);
+            if (x0 + V >= w) {                   // the row's last chunk (rare)
+                int cls;
+                const unsigned short* prow = src + i * PL + int64_t(source_row(y, dr, h, ym, &cls)) * P;
+#pragma unroll
+                for (int k = 0; k < V; ++k) {
+                    const int sx = x0 + k + 1;
+                    if (sx >= w) {
+                        if (xper) {
+                            if (!(k == V - 1 && sx == w))
+                                set_packed<NP>(r[i], k, __ldg(prow + (sx % w)));
+                        } else if (xm == 2) {
+                            xb |= 1u << k;
+                        } else {
+                            xz |= 1u << k;
+                        }
+                    }
+                }
+            }
+        }
+        int cls;
+        (void)source_row(y, dr, h, ym, &cls);
+        uint32_t b = (cls == 2) ? FULL : xb;
+        const uint32_t z = (cls == 1 ? FULL : xz) & ~b;
+        if (has_solid && halfway) b |= (mrow[1 - dr] >> (1 - dc)) & FULL;
+        zb[i] = z & ~b;                          // a bounce-back link overrides padding
+        bnc[i] = b;
+    }
+
+    // ---- phase C: bounce-back links take the cell's own opposite population
+#pragma unroll
+    for (int i = 1; i < 9; ++i) {
+        if (bnc[i]) {
+            uint32_t own[NP];
+            PackIO<NP>::load(src + OPP(i) * PL + int64_t(y) * P + xl, own);
+#pragma unroll
+            for (int j = 0; j < NP; ++j) {
+                const uint32_t m = half_mask(bnc[i], j);
+                r[i][j] = (r[i][j] & ~m) | (own[j] & m);
+            }
+        }
+    }
+    const uint32_t own_solid = has_solid ? ((mrow[1] >> 1) & FULL) : 0u;
+    if (own_solid && !halfway) {
+        // bounce_back (src/lbm.rs:741-751): solid nodes take swapped
+        // populations; a zero-padded link moves with its value (w_i equals
+        // w_opp(i), so the substitute is the same)
+#pragma unroll
+        for (int p = 0; p < 4; ++p) {
+            const int i0 = p < 2 ? 1 + p : 5 + (p - 2), i1 = OPP(i0);
+#pragma unroll
+            for (int j = 0; j < NP; ++j) {
+                const uint32_t m = half_mask(own_solid, j);
+                const uint32_t t = (r[i0][j] ^ r[i1][j]) & m;
+                r[i0][j] ^= t;
+                r[i1][j] ^= t;
+            }
+            const uint32_t t = (zb[i0] ^ zb[i1]) & own_solid;
+            zb[i0] ^= t;
+            zb[i1] ^= t;
+        }
+    }
+
+    // ---- phase D: collide and write ---------------------------------------
+    const uint32_t past = x0 + V > w ? (FULL << (w - x0 > 0 ? w - x0 : 0)) & FULL : 0u;
+    collide_packed<S, V, SR, true>(a.c, r, zb, past);
+    if (own_solid && halfway) {
+        // half-way mode: solid nodes keep their populations
+#pragma unroll
+        for (int i = 0; i < 9; ++i) {
+            uint32_t own[NP];
+            PackIO<NP>::load(src + i * PL + int64_t(y) * P + xl, own);
+#pragma unroll
+            for (int j = 0; j < NP; ++j) {
+                const uint32_t m = half_mask(own_solid, j);
+                r[i][j] = (r[i][j] & ~m) | (own[j] & m);
+            }
+        }
+    }
+    if (!active) return;
+    store_packed<S, V>(a, y, x0, r);
+}
+
 // One step over the whole lattice in one launch.  With tile flags: the first
 // ceil(ngtiles / rows) blocks take the flagged tiles from the list a.gtiles
 // (entry = row * ntiles + tile), one warp per entry, so their longer latency
@@ -771,10 +1194,20 @@ __device__ __forceinline__ void step_general(const StepArgs<typename Store<S>::C
 #ifndef LBM_STEP_MIN_BLOCKS_16
 #define LBM_STEP_MIN_BLOCKS_16 3
 #endif
+#ifndef LBM_PACKED16
+#define LBM_PACKED16 1
+#endif
+#ifndef LBM_STEP_MIN_BLOCKS_16_V8
+#define LBM_STEP_MIN_BLOCKS_16_V8 2
+#endif
+template <class S, int V>
+constexpr int step_min_blocks() {
+    if (sizeof(typename Store<S>::CT) != 4) return 1;
+    if (sizeof(S) == 2) return V <= 4 ? LBM_STEP_MIN_BLOCKS_16 : LBM_STEP_MIN_BLOCKS_16_V8;
+    return V <= 4 ? LBM_STEP_MIN_BLOCKS : 1;
+}
 template <class S, int V, int FRAME, bool FAST, bool SR>
-__global__ void __launch_bounds__(256, (sizeof(typename Store<S>::CT) == 4 && V <= 4)
-                                           ? (sizeof(S) == 2 ? LBM_STEP_MIN_BLOCKS_16 : LBM_STEP_MIN_BLOCKS)
-                                           : 1)
+__global__ void __launch_bounds__(256, step_min_blocks<S, V>())
 lbm_step_kernel(const StepArgs<typename Store<S>::CT> a) {
     const int rows = blockDim.y;
     const int gblocks = a.tflags != nullptr ? (a.ngtiles + rows - 1) / rows : 0;
@@ -784,7 +1217,9 @@ lbm_step_kernel(const StepArgs<typename Store<S>::CT> a) {
         if (e >= a.ngtiles) return;
         const uint32_t t = a.gtiles[e];
         const int y = int(t / uint32_t(a.ntiles));
-        step_general<S, V, FRAME, FAST, SR>(a, y, int(t - uint32_t(y) * uint32_t(a.ntiles)), threadIdx.x);
+        const int tile = int(t - uint32_t(y) * uint32_t(a.ntiles));
+        if constexpr (Store<S>::DEV && LBM_PACKED16) step_general_packed<S, V, FRAME, SR>(a, y, tile, threadIdx.x);
+        else step_general<S, V, FRAME, FAST, SR>(a, y, tile, threadIdx.x);
         return;
     }
     const int ib = b - gblocks;
@@ -792,14 +1227,28 @@ lbm_step_kernel(const StepArgs<typename Store<S>::CT> a) {
     const int y = by * rows + threadIdx.y;
     if (y >= a.h) return;                                                  // warp-uniform
     if (a.tflags == nullptr) {
-        step_general<S, V, FRAME, FAST, SR>(a, y, tile, threadIdx.x);
+        if constexpr (Store<S>::DEV && LBM_PACKED16) step_general_packed<S, V, FRAME, SR>(a, y, tile, threadIdx.x);
+        else step_general<S, V, FRAME, FAST, SR>(a, y, tile, threadIdx.x);
         return;
     }
     const uint8_t flag = a.tflags[int64_t(y) * a.ntiles + tile];        // warp-uniform
     if (flag == 1) return;                                                 // owned by the list
-    if (flag == 0) step_interior<S, V, FRAME, FAST, SR>(a, y, (tile * 32 + threadIdx.x) * V, threadIdx.x);
-    else step_interior_wrap<S, V, FRAME, FAST, SR>(a, y, (tile * 32 + threadIdx.x) * V, threadIdx.x);
+    const int x0 = (tile * 32 + threadIdx.x) * V;
+    if constexpr (Store<S>::DEV && LBM_PACKED16) {
+        if (flag == 0) step_interior_packed<S, V, FRAME, SR>(a, y, x0, threadIdx.x);
+        else step_interior_wrap_packed<S, V, FRAME, SR>(a, y, x0, threadIdx.x);
+    } else {
+        if (flag == 0) step_interior<S, V, FRAME, FAST, SR>(a, y, x0, threadIdx.x);
+        else step_interior_wrap<S, V, FRAME, FAST, SR>(a, y, x0, threadIdx.x);
+    }
 }
+
+// Prefetch distance, in percent of the rows the resident blocks cover (the
+// wavefront's depth): far enough that the prefetched rows arrive before
+// their warps start, near enough that they are still in L2.
+#ifndef LBM_PREFETCH_PCT
+#define LBM_PREFETCH_PCT 60
+#endif
 
 template <class S, int V, int FRAME, bool FAST, bool SR>
 void launch_step_tv(const StepArgs<typename Store<S>::CT>& a, int rows, cudaStream_t stream) {
@@ -808,6 +1257,22 @@ void launch_step_tv(const StepArgs<typename Store<S>::CT>& a, int rows, cudaStre
     const int gblocks = a.tflags != nullptr ? (a.ngtiles + rows - 1) / rows : 0;
     StepArgs<typename Store<S>::CT> b = a;
     b.ntiles = ntiles;
+    if (b.pf_rows < 0) {
+        // resident blocks per SM of this kernel at this block size, and SMs
+        // (cached per instantiation; the same GPU model throughout)
+        static int occ[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        static int sms = 0;
+        if (sms == 0) {
+            int dev = 0;
+            if (cudaGetDevice(&dev) == cudaSuccess)
+                cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        }
+        if (occ[rows] == 0)
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[rows], lbm_step_kernel<S, V, FRAME, FAST, SR>,
+                                                          32 * rows, 0);
+        const int64_t wave_rows = int64_t(occ[rows]) * sms * rows / ntiles;
+        b.pf_rows = int(wave_rows * LBM_PREFETCH_PCT / 100);
+    }
     lbm_step_kernel<S, V, FRAME, FAST, SR><<<gblocks + ntiles * rowblocks, dim3(32, rows), 0, stream>>>(b);
 }
 

@@ -71,7 +71,7 @@ extern "C" {
 #define LBM_FAST        0x40 /* FMA-contracted, algebraically simplified collision
                                 instead of the reference's operation order        */
 /* 16-bit deviation storage rounds collided values stochastically by default
- * (a reproducible offset hashed from the value's own bits): round-to-nearest
+ * (random bits from the stored pair's own f32 bits, so runs reproduce): round-to-nearest
  * repeats the same error step after step on a slowly changing field, and
  * those errors add up.  This flag selects round-to-nearest (faster, less
  * accurate over long runs).  Ignored by f32 and f64 storage.               */
@@ -206,8 +206,9 @@ int lbm_check_device_noalloc(const void* populations, int precision, int w, int 
                              int row_pitch, int64_t plane_stride, float delta_x,
                              float delta_t, void* stream, lbm_health* out);
 
-/* Tile of the fused step: cells per thread along x (f32: 2, 4 or 8; f64: 2;
- * 16-bit: 4 or 8) and warps (rows) per block (1..8); 0 keeps the default.
+/* Tile of the fused step: cells per thread along x (f32: 2, 4 or 8, default
+ * 4; f64: 2; 16-bit: 4 or 8, default 8) and warps (rows) per block (1..8,
+ * default 4); 0 keeps the default.
  * No reference counterpart (tuning knob of the GB300 kernel).            */
 int lbm_set_tile(lbm_lattice* lat, int cells_per_thread, int rows_per_block);
 

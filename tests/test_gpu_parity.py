@@ -457,3 +457,93 @@ def test_async_moment_readback_is_a_snapshot(gpu):
         a.readback_wait()
         b.step(7)
         assert np.array_equal(pin[1], b.moments()[1])
+
+
+# -- interior paths against the general path ---------------------------------
+
+def _raw_planes(lat, path):
+    """The stored populations bit for bit (the checkpoint's planes)."""
+    lat.save(str(path))
+    es = 4 if lat.precision == F32 else 2
+    return np.fromfile(str(path), dtype=np.uint32 if es == 4 else np.uint16,
+                       count=9 * lat.w * lat.h, offset=96).reshape(9, lat.h, lat.w)
+
+
+@pytest.mark.parametrize("precision,extra", [(F16DEV, 0), (F16DEV, lbm.ROUND_NEAREST),
+                                             (BF16DEV, 0), (F32, 0)])
+@pytest.mark.parametrize("cells", [4, 8])
+@pytest.mark.parametrize("frame", [0, FRAME_XY])
+@pytest.mark.parametrize("collision", [0, COLLISION_TRT])
+def test_interior_paths_match_general_path(gpu, tmp_path, precision, extra, cells, frame,
+                                           collision):
+    """One step from the same random state: every cell whose periodic 3 x 3
+    neighbourhood holds no solid gets the same stored bits whether its warp
+    tile runs an interior path (no solids anywhere: lean and periodic-edge
+    tiles) or the general path (sparse solids flag most tiles)."""
+    w, h = 32 * cells * 3 + 37, 40          # a partial last tile
+    flags = X_PERIODIC | Y_PERIODIC | frame | FAST | extra
+    rng = np.random.default_rng(cells + 7 * frame)
+    solid = np.zeros((h, w), np.uint8)
+    solid[rng.integers(0, h, 60), rng.integers(0, w, 60)] = 1
+    near = np.zeros((h, w), bool)
+    for dy in (-1, 0, 1):
+        for dx in (-1, 0, 1):
+            near |= np.roll(np.roll(solid, dy, 0), dx, 1).astype(bool)
+    f0 = random_state(w, h, np.float32, seed=5)
+    out = []
+    for k, geom in enumerate((None, solid)):
+        with Lattice(w, h, 0.7, precision, flags) as lat:
+            if collision:
+                lat.set_collision(collision, 0.7, 0.9)
+            lat.set_force(3e-5, -1e-5)
+            if geom is not None:
+                lat.set_geometry(geom)
+            lat.set_tile(cells, 4)
+            lat.set_populations(f0)
+            lat.step(1)
+            out.append(_raw_planes(lat, tmp_path / f"s{k}.lbm"))
+    # warp tiles (row, 32 * cells columns) whose pull neighbourhood holds a solid
+    tw = 32 * cells
+    ntiles = -(-w // tw)
+    flagged = np.zeros((h, ntiles), bool)
+    for y, x in zip(*np.nonzero(solid)):
+        for t in {(x - 1) % w // tw, x // tw, (x + 1) % w // tw}:
+            flagged[[(y - 1) % h, y, (y + 1) % h], t] = True
+    keep = ~near
+    assert flagged.mean() > 0.5 and keep.mean() > 0.8
+    diff = (out[0] != out[1]) & keep
+    where = np.argwhere(diff)
+    assert where.size == 0, (f"{len(where)} values differ, first (i, y, x): {where[:8].tolist()}; "
+                             f"interior {out[0][diff][:8].tolist()} general {out[1][diff][:8].tolist()}")
+
+
+@pytest.mark.parametrize("precision,tol", [(F16DEV, 3e-4), (BF16DEV, 4e-3)])
+@pytest.mark.parametrize("edges", [X_WALL | Y_WALL, X_PERIODIC | Y_WALL | SOLID_HALFWAY, 0,
+                                   X_WALL | Y_PERIODIC | SOLID_HALFWAY, X_PERIODIC | Y_PERIODIC])
+@pytest.mark.parametrize("frame", [0, FRAME_XY])
+@pytest.mark.parametrize("cells", [4, 8])
+def test_deviation_storage_boundaries_one_step(gpu, precision, tol, edges, frame, cells):
+    """One step of 16-bit storage against the f64 oracle from the same
+    (decoded) state, with walls, zero padding, periodic edges, solids (full-
+    and half-way), a body force and TRT: every population within the format's
+    rounding.  A wrong boundary rule moves populations by O(1e-2)."""
+    w, h = 32 * cells + 45, 37
+    flags = edges | frame | FAST
+    rng = np.random.default_rng(11)
+    solid = (rng.uniform(size=(h, w)) < 0.04).astype(np.uint8)
+    solid[10:20, 30:50] = 1
+    f0 = random_state(w, h, np.float64, seed=12, du=0.1)
+    with Lattice(w, h, 0.7, precision, flags) as lat:
+        lat.set_collision(COLLISION_TRT, 0.7, 0.85)
+        lat.set_force(2e-4, -1e-4)
+        lat.set_geometry(solid)
+        lat.set_tile(cells, 4)
+        lat.set_populations(f0.astype(np.float32))
+        start = lat.get_populations(np.float64)
+        lat.step(1)
+        got = lat.get_populations(np.float64)
+    want = oracle.step(start, 1, tau=0.7, flags=flags & ~FAST, collision=COLLISION_TRT,
+                       tau_minus=0.85, force=(2e-4, -1e-4), solid=solid)
+    err = np.abs(got - want)
+    assert np.all(np.isfinite(got))
+    assert err.max() <= tol, f"max error {err.max():.3e} at {np.unravel_index(err.argmax(), err.shape)}"
