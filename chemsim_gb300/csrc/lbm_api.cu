@@ -205,9 +205,14 @@ int refresh_tiles(lbm_lattice* L) {
     LBM_CUDA(cudaMemcpyAsync(flags.data(), L->tflags, flags.size(), cudaMemcpyDeviceToHost,
                              L->stream));
     LBM_CUDA(cudaStreamSynchronize(L->stream));
+    // Entries of tiles flagged 3 carry bit 31 (the general path without edge
+    // handling); row * ntiles + tile stays below 2^31 (h <= 65535 * 8 rows).
     std::vector<uint32_t> list;
-    for (int64_t t = 0; t < n; ++t)
-        if (flags[size_t(t)] == 1) list.push_back(uint32_t(t));
+    for (int64_t t = 0; t < n; ++t) {
+        const uint8_t f = flags[size_t(t)];
+        if (f == 1) list.push_back(uint32_t(t));
+        else if (f == 3) list.push_back(uint32_t(t) | 0x80000000u);
+    }
     if (list.size() > L->gtiles_cap) {
         if (L->gtiles) cudaFree(L->gtiles);
         L->gtiles = nullptr;
@@ -434,6 +439,7 @@ __global__ void tile_flags_kernel(uint8_t* __restrict__ tflags, const uint8_t* _
         const bool xedge = xs == 0 || xs + tile_w >= w;
         const bool yedge = y == 0 || y == h - 1;
         bool gen = (xedge && !xper) || (yedge && !yper);
+        bool solid_gen = false;
         if (!gen && solid != nullptr) {
             const int xe = min(xs + tile_w, w);          // columns xs-1 .. xe, wrapped
             for (int r = y - 1; r <= y + 1 && !gen; ++r) {
@@ -441,11 +447,13 @@ __global__ void tile_flags_kernel(uint8_t* __restrict__ tflags, const uint8_t* _
                 const uint8_t* row = solid + int64_t(rr) * mpitch;
                 for (int c = xs - 1; c <= xe; ++c) {
                     const int cc = c < 0 ? c + w : (c >= w ? c - w : c);
-                    if (row[cc]) { gen = true; break; }
+                    if (row[cc]) { gen = solid_gen = true; break; }
                 }
             }
         }
-        tflags[t] = gen ? 1 : ((xedge || yedge) ? 2 : 0);
+        // 3: solids nearby but every source cell inside the lattice (the
+        // general path without edge handling); 1: the full general path
+        tflags[t] = gen ? ((solid_gen && !xedge && !yedge) ? 3 : 1) : ((xedge || yedge) ? 2 : 0);
     }
 }
 

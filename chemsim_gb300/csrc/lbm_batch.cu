@@ -153,7 +153,7 @@ int ensure_table(lbm_batch* B) {
         for (int r = 0; r < L->h; ++r)
             for (int t = 0; t < L->ntiles; ++t) {
                 const uint8_t fl = flags[size_t(r) * L->ntiles + t];
-                const int j = fl == 1 ? 0 : (fl == 2 ? 1 : 2);
+                const int j = (fl & 1) ? 0 : (fl == 2 ? 1 : 2);     // 1, 3: general
                 lists[vbase + j].push_back(make_uint2(uint32_t(i), (uint32_t(r) << 12) | uint32_t(t)));
             }
     }

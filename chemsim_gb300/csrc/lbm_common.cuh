@@ -211,9 +211,9 @@ struct StepArgs {
     const void* src;        // 9 planes, current state
     void* dst;              // 9 planes, next state
     const uint8_t* solid;   // mask (pitch mpitch) or null
-    const uint8_t* tflags;  // per (row, warp tile): 1 = boundary/solid nearby, or null
+    const uint8_t* tflags;  // per (row, warp tile): 0 interior, 2 periodic edge, 1 / 3 listed, or null
     int ntiles;             // warp tiles per row (row stride of tflags)
-    const uint32_t* gtiles; // flagged tiles (row * ntiles + tile), or null
+    const uint32_t* gtiles; // listed tiles (row * ntiles + tile, bit 31: no lattice edge in reach), or null
     int ngtiles;
     float* mom_rho;         // moment outputs (pitch `pitch`) or null
     float* mom_ux;

@@ -29,6 +29,21 @@ namespace lbmk {
 
 constexpr unsigned kFull = 0xffffffffu;
 
+// 16-bit storage keeps values packed two per register through the shifts
+// (LBM_PACKED16 = 0 selects the plain form).  At 8 cells per thread the
+// periodic-edge path collides its pairs in a loop that is not unrolled
+// (LBM_ROLL_WRAP; the general paths always do): less code for the instruction
+// cache, measured 1% faster; unrolled is faster for the interior path.
+#ifndef LBM_PACKED16
+#define LBM_PACKED16 1
+#endif
+#ifndef LBM_ROLL_INTERIOR
+#define LBM_ROLL_INTERIOR 0
+#endif
+#ifndef LBM_ROLL_WRAP
+#define LBM_ROLL_WRAP 1
+#endif
+
 template <class S, int V>
 struct VecIO {
     static constexpr int BYTES = int(sizeof(S)) * V;
@@ -652,7 +667,11 @@ __device__ __forceinline__ void set_packed(uint32_t (&r)[NP], int k, uint32_t e)
 // With SUB (general tiles), zero-padded links (bit k of zb[i]) take the
 // deviation value of f = 0 after widening, and cells past the lattice edge
 // (bit k of past) collide zeros under stochastic rounding (zero_past_edge).
-template <class S, int V, bool SR, bool SUB = false>
+// With ROLL the pairs are taken in a loop that is not unrolled: each pass
+// collides register 0 of every plane and rotates the registers down, so the
+// collision's code appears once (the general paths, where code size and not
+// the rotation's moves is what costs).
+template <class S, int V, bool SR, bool SUB = false, bool ROLL = false>
 __device__ __forceinline__ void collide_packed(const Consts<float>& c, uint32_t (&r)[9][V / 2],
                                                const uint32_t* zb = nullptr, uint32_t past = 0u) {
     using ST = Store<S>;
@@ -662,6 +681,44 @@ __device__ __forceinline__ void collide_packed(const Consts<float>& c, uint32_t 
     if constexpr (SUB) {
 #pragma unroll
         for (int i = 0; i < 9; ++i) any |= zb[i];
+    }
+    if constexpr (ROLL) {
+        uint32_t zl[9];
+#pragma unroll
+        for (int i = 0; i < 9; ++i) zl[i] = SUB ? zb[i] : 0u;
+        uint32_t pl = past;
+#pragma unroll 1
+        for (int j = 0; j < NP; ++j) {
+            float2 g[9], o[9];
+#pragma unroll
+            for (int i = 0; i < 9; ++i) {
+                H2 p;
+                memcpy(&p, &r[i][0], 4);
+                g[i] = ST::to_f2(p);
+            }
+            if (SUB && (any & 3u)) {
+#pragma unroll
+                for (int i = 0; i < 9; ++i) {
+                    const float zv = ST::zero_dom(c.wt[i], c.dscale);
+                    if (zl[i] & 1u) g[i].x = zv;
+                    if (zl[i] & 2u) g[i].y = zv;
+                    if (SR && (pl & 1u)) g[i].x = 0.f;
+                    if (SR && (pl & 2u)) g[i].y = 0.f;
+                }
+            }
+            collide_dev_x2(c, g, o);
+#pragma unroll
+            for (int i = 0; i < 9; ++i) {
+                const H2 p = SR ? ST::from_f2_sr(o[i].x, o[i].y) : ST::from_f2(o[i]);
+#pragma unroll
+                for (int k = 0; k < NP - 1; ++k) r[i][k] = r[i][k + 1];
+                memcpy(&r[i][NP - 1], &p, 4);
+                zl[i] >>= 2;
+            }
+            pl >>= 2;
+            any >>= 2;
+        }
+        return;
     }
 #pragma unroll
     for (int j = 0; j < NP; ++j) {
@@ -710,10 +767,10 @@ __device__ __forceinline__ void store_packed(const StepArgs<float>& a, int y, in
     store_cells<S, V, true>(a, y, x0, enc);
 }
 
-template <class S, int V, bool SR>
+template <class S, int V, bool SR, bool ROLL = false>
 __device__ __forceinline__ void collide_store_packed(const StepArgs<float>& a, int y, int x0,
                                                      uint32_t (&r)[9][V / 2]) {
-    collide_packed<S, V, SR>(a.c, r);
+    collide_packed<S, V, SR, false, ROLL>(a.c, r);
     store_packed<S, V>(a, y, x0, r);
 }
 
@@ -752,7 +809,7 @@ __device__ __forceinline__ void step_interior_packed(const StepArgs<float>& a, i
             shift_down_packed<NP>(r[i], lane == 31 ? edge[i] : right);
         }
     }
-    collide_store_packed<S, V, SR>(a, y, x0, r);
+    collide_store_packed<S, V, SR, (V / 2 >= 4) && LBM_ROLL_INTERIOR>(a, y, x0, r);
 }
 
 // Periodic-edge warp tile (flag 2) of 16-bit storage, packed (the rules of
@@ -806,7 +863,7 @@ __device__ __forceinline__ void step_interior_wrap_packed(const StepArgs<float>&
             for (int k = 0; k < V; ++k)
                 if (x0 + k >= w) set_packed<NP>(r[i], k, 0u);
     }
-    collide_store_packed<S, V, SR>(a, y, x0, r);
+    collide_store_packed<S, V, SR, (V / 2 >= 4) && LBM_ROLL_WRAP>(a, y, x0, r);
 }
 
 // One time step of one lattice.  Phase A issues every global load of the
@@ -816,7 +873,7 @@ __device__ __forceinline__ void step_interior_wrap_packed(const StepArgs<float>&
 // classifies boundary links; phase C fetches the cell's own opposite
 // populations for bounce-back links (only near walls and solids); phase D
 // collides and stores.
-template <class S, int V, int FRAME, bool FAST, bool SR = false>
+template <class S, int V, int FRAME, bool FAST, bool SR = false, bool EDGE = true>
 __device__ __forceinline__ void step_general(const StepArgs<typename Store<S>::CT>& a, int y,
                                              int tile, int lane) {
     using CT = typename Store<S>::CT;
@@ -834,8 +891,8 @@ __device__ __forceinline__ void step_general(const StepArgs<typename Store<S>::C
     const bool halfway = (a.flags & LBM_SOLID_HALFWAY) != 0;
     const bool has_solid = a.solid != nullptr;
     const bool xper = xm == 1;
-    const bool left_edge = lane == 0 || x0 == 0;          // needs column x0 - 1 itself
-    const bool right_edge = lane == 31 || x0 + V >= w;    // needs column x0 + V itself
+    const bool left_edge = lane == 0 || (EDGE && x0 == 0);          // needs column x0 - 1 itself
+    const bool right_edge = lane == 31 || (EDGE && x0 + V >= w);    // needs column x0 + V itself
 
     // ---- phase A: issue all loads ----------------------------------------
     uint32_t mcore[3] = {0u, 0u, 0u}, mleft[3] = {0u, 0u, 0u}, mright[3] = {0u, 0u, 0u};
@@ -844,15 +901,15 @@ __device__ __forceinline__ void step_general(const StepArgs<typename Store<S>::C
         for (int r = 0; r < 3; ++r) {
             int row = y - 1 + r;
             bool ok = true;
-            if (row < 0 || row >= h) {
+            if (EDGE && (row < 0 || row >= h)) {
                 if (ym == 1) row = row < 0 ? row + h : row - h;
                 else ok = false;
             }
             if (ok) {   // warp-uniform
                 const uint8_t* mr = a.solid + int64_t(row) * a.mpitch;
                 mcore[r] = load_mask_core<V>(mr + xl);
-                if (left_edge) mleft[r] = mask_at(mr, x0 - 1, w, xper);
-                if (right_edge) mright[r] = mask_at(mr, x0 + V, w, xper);
+                if (left_edge) mleft[r] = EDGE ? mask_at(mr, x0 - 1, w, xper) : __ldg(mr + x0 - 1);
+                if (right_edge) mright[r] = EDGE ? mask_at(mr, x0 + V, w, xper) : __ldg(mr + x0 + V);
             }
         }
     }
@@ -862,18 +919,18 @@ __device__ __forceinline__ void step_general(const StepArgs<typename Store<S>::C
 #pragma unroll
     for (int i = 0; i < 9; ++i) {
         const int dc = DCOL(FRAME, i), dr = DROW(FRAME, i);
-        int cls;
-        const int sr = source_row(y, dr, h, ym, &cls);
+        int cls = 0;
+        const int sr = EDGE ? source_row(y, dr, h, ym, &cls) : y - dr;
         const S* prow = src + i * PL + int64_t(sr) * P;
         IO::load(prow + xl, raw[i]);
         edge[i] = raw[i][0];
         if (dc == 1) {
             int ec = x0 - 1;
-            if (ec < 0) ec = xper ? w - 1 : -1;
+            if (EDGE && ec < 0) ec = xper ? w - 1 : -1;
             if (left_edge && ec >= 0) edge[i] = __ldg(prow + ec);
         } else if (dc == -1) {
             int ec = x0 + V;
-            if (ec >= w) ec = (xper && ec == w) ? 0 : -1;
+            if (EDGE && ec >= w) ec = (xper && ec == w) ? 0 : -1;
             if (right_edge && ec >= 0) edge[i] = __ldg(prow + ec);
         }
     }
@@ -886,7 +943,7 @@ __device__ __forceinline__ void step_general(const StepArgs<typename Store<S>::C
             uint32_t core = mcore[r];
             const uint32_t l = __shfl_up_sync(kFull, (core >> (V - 1)) & 1u, 1);
             const uint32_t rr = __shfl_down_sync(kFull, core & 1u, 1);
-            if (x0 + V > w && xper) {            // partial last chunk, periodic: wrap
+            if (EDGE && x0 + V > w && xper) {    // partial last chunk, periodic: wrap
                 int row = y - 1 + r;
                 if (row < 0) row += h;
                 if (row >= h) row -= h;
@@ -914,13 +971,13 @@ __device__ __forceinline__ void step_general(const StepArgs<typename Store<S>::C
 #pragma unroll
             for (int k = V - 1; k > 0; --k) v[k] = v[k - 1];
             v[0] = left_edge ? e : left;
-            if (x0 == 0 && !xper) { if (xm == 2) xb |= 1u; else xz |= 1u; }
+            if (EDGE && x0 == 0 && !xper) { if (xm == 2) xb |= 1u; else xz |= 1u; }
         } else if (dc == -1) {
             const CT right = __shfl_down_sync(kFull, v[0], 1);
 #pragma unroll
             for (int k = 0; k < V - 1; ++k) v[k] = v[k + 1];
             v[V - 1] = right_edge ? e : right;
-            if (x0 + V >= w) {                   // the row's last chunk (rare)
+            if (EDGE && x0 + V >= w) {           // the row's last chunk (rare)
                 int cls;
                 const S* prow = src + i * PL + int64_t(source_row(y, dr, h, ym, &cls)) * P;
 #pragma unroll
@@ -939,8 +996,8 @@ __device__ __forceinline__ void step_general(const StepArgs<typename Store<S>::C
                 }
             }
         }
-        int cls;
-        (void)source_row(y, dr, h, ym, &cls);
+        int cls = 0;
+        if (EDGE) (void)source_row(y, dr, h, ym, &cls);
         uint32_t b = (cls == 2) ? FULL : xb;
         const uint32_t z = (cls == 1 ? FULL : xz) & ~b;
         if (has_solid && halfway) b |= (mrow[1 - dr] >> (1 - dc)) & FULL;
@@ -982,7 +1039,7 @@ __device__ __forceinline__ void step_general(const StepArgs<typename Store<S>::C
     }
 
     // ---- phase D: collide and write ---------------------------------------
-    if (SR && x0 + V > w) zero_past_edge<S, V>(f, x0, w);
+    if (EDGE && SR && x0 + V > w) zero_past_edge<S, V>(f, x0, w);
     S enc[9][V];
     collide_cells<S, V, FAST>(a.c, f);
 #pragma unroll
@@ -1009,7 +1066,7 @@ __device__ __forceinline__ void step_general(const StepArgs<typename Store<S>::C
 // half-way keep move raw 16-bit values (exact in either form); zero-padded
 // links are substituted after widening, where the value f = 0 has its exact
 // f32 deviation form.
-template <class S, int V, int FRAME, bool SR>
+template <class S, int V, int FRAME, bool SR, bool EDGE = true>
 __device__ __forceinline__ void step_general_packed(const StepArgs<float>& a, int y, int tile,
                                                     int lane) {
     constexpr int NP = V / 2;
@@ -1024,8 +1081,8 @@ __device__ __forceinline__ void step_general_packed(const StepArgs<float>& a, in
     const bool halfway = (a.flags & LBM_SOLID_HALFWAY) != 0;
     const bool has_solid = a.solid != nullptr;
     const bool xper = xm == 1;
-    const bool left_edge = lane == 0 || x0 == 0;
-    const bool right_edge = lane == 31 || x0 + V >= w;
+    const bool left_edge = lane == 0 || (EDGE && x0 == 0);
+    const bool right_edge = lane == 31 || (EDGE && x0 + V >= w);
 
     // ---- phase A: issue all loads ----------------------------------------
     uint32_t mcore[3] = {0u, 0u, 0u}, mleft[3] = {0u, 0u, 0u}, mright[3] = {0u, 0u, 0u};
@@ -1034,15 +1091,15 @@ __device__ __forceinline__ void step_general_packed(const StepArgs<float>& a, in
         for (int r = 0; r < 3; ++r) {
             int row = y - 1 + r;
             bool ok = true;
-            if (row < 0 || row >= h) {
+            if (EDGE && (row < 0 || row >= h)) {
                 if (ym == 1) row = row < 0 ? row + h : row - h;
                 else ok = false;
             }
             if (ok) {
                 const uint8_t* mr = a.solid + int64_t(row) * a.mpitch;
                 mcore[r] = load_mask_core<V>(mr + xl);
-                if (left_edge) mleft[r] = mask_at(mr, x0 - 1, w, xper);
-                if (right_edge) mright[r] = mask_at(mr, x0 + V, w, xper);
+                if (left_edge) mleft[r] = EDGE ? mask_at(mr, x0 - 1, w, xper) : __ldg(mr + x0 - 1);
+                if (right_edge) mright[r] = EDGE ? mask_at(mr, x0 + V, w, xper) : __ldg(mr + x0 + V);
             }
         }
     }
@@ -1051,18 +1108,18 @@ __device__ __forceinline__ void step_general_packed(const StepArgs<float>& a, in
 #pragma unroll
     for (int i = 0; i < 9; ++i) {
         const int dc = DCOL(FRAME, i), dr = DROW(FRAME, i);
-        int cls;
-        const int sr = source_row(y, dr, h, ym, &cls);
+        int cls = 0;
+        const int sr = EDGE ? source_row(y, dr, h, ym, &cls) : y - dr;
         const unsigned short* prow = src + i * PL + int64_t(sr) * P;
         PackIO<NP>::load(prow + xl, r[i]);
         edge[i] = 0u;
         if (dc == 1) {
             int ec = x0 - 1;
-            if (ec < 0) ec = xper ? w - 1 : -1;
+            if (EDGE && ec < 0) ec = xper ? w - 1 : -1;
             if (left_edge && ec >= 0) edge[i] = uint32_t(__ldg(prow + ec)) << 16;
         } else if (dc == -1) {
             int ec = x0 + V;
-            if (ec >= w) ec = (xper && ec == w) ? 0 : -1;
+            if (EDGE && ec >= w) ec = (xper && ec == w) ? 0 : -1;
             if (right_edge && ec >= 0) edge[i] = __ldg(prow + ec);
         }
     }
@@ -1075,7 +1132,7 @@ __device__ __forceinline__ void step_general_packed(const StepArgs<float>& a, in
             uint32_t core = mcore[q];
             const uint32_t l = __shfl_up_sync(kFull, (core >> (V - 1)) & 1u, 1);
             const uint32_t rr = __shfl_down_sync(kFull, core & 1u, 1);
-            if (x0 + V > w && xper) {
+            if (EDGE && x0 + V > w && xper) {
                 int row = y - 1 + q;
                 if (row < 0) row += h;
                 if (row >= h) row -= h;
@@ -1095,11 +1152,11 @@ __device__ __forceinline__ void step_general_packed(const StepArgs<float>& a, in
         if (dc == 1) {
             const uint32_t left = __shfl_up_sync(kFull, r[i][NP - 1], 1);
             shift_up_packed<NP>(r[i], left_edge ? edge[i] : left);
-            if (x0 == 0 && !xper) { if (xm == 2) xb |= 1u; else xz |= 1u; }
+            if (EDGE && x0 == 0 && !xper) { if (xm == 2) xb |= 1u; else xz |= 1u; }
         } else if (dc == -1) {
             const uint32_t right = __shfl_down_sync(kFull, r[i][0], 1);
             shift_down_packed<NP>(r[i], right_edge ? edge[i] : right);
-            if (x0 + V >= w) {                   // the row's last chunk (rare)
+            if (EDGE && x0 + V >= w) {           // the row's last chunk (rare)
                 int cls;
                 const unsigned short* prow = src + i * PL + int64_t(source_row(y, dr, h, ym, &cls)) * P;
 #pragma unroll
@@ -1118,8 +1175,8 @@ __device__ __forceinline__ void step_general_packed(const StepArgs<float>& a, in
                 }
             }
         }
-        int cls;
-        (void)source_row(y, dr, h, ym, &cls);
+        int cls = 0;
+        if (EDGE) (void)source_row(y, dr, h, ym, &cls);
         uint32_t b = (cls == 2) ? FULL : xb;
         const uint32_t z = (cls == 1 ? FULL : xz) & ~b;
         if (has_solid && halfway) b |= (mrow[1 - dr] >> (1 - dc)) & FULL;
@@ -1162,8 +1219,8 @@ __device__ __forceinline__ void step_general_packed(const StepArgs<float>& a, in
     }
 
     // ---- phase D: collide and write ---------------------------------------
-    const uint32_t past = x0 + V > w ? (FULL << (w - x0 > 0 ? w - x0 : 0)) & FULL : 0u;
-    collide_packed<S, V, SR, true>(a.c, r, zb, past);
+    const uint32_t past = (EDGE && x0 + V > w) ? (FULL << (w - x0 > 0 ? w - x0 : 0)) & FULL : 0u;
+    collide_packed<S, V, SR, true, (V / 2 >= 4)>(a.c, r, zb, past);
     if (own_solid && halfway) {
         // half-way mode: solid nodes keep their populations
 #pragma unroll
@@ -1181,6 +1238,13 @@ __device__ __forceinline__ void step_general_packed(const StepArgs<float>& a, in
     store_packed<S, V>(a, y, x0, r);
 }
 
+// A listed (general) tile.
+template <class S, int V, int FRAME, bool FAST, bool SR, bool EDGE>
+__device__ __forceinline__ void step_listed(const StepArgs<typename Store<S>::CT>& a, int y, int tile) {
+    if constexpr (Store<S>::DEV && LBM_PACKED16) step_general_packed<S, V, FRAME, SR, EDGE>(a, y, tile, threadIdx.x);
+    else step_general<S, V, FRAME, FAST, SR, EDGE>(a, y, tile, threadIdx.x);
+}
+
 // One step over the whole lattice in one launch.  With tile flags: the first
 // ceil(ngtiles / rows) blocks take the flagged tiles from the list a.gtiles
 // (entry = row * ntiles + tile), one warp per entry, so their longer latency
@@ -1193,9 +1257,6 @@ __device__ __forceinline__ void step_general_packed(const StepArgs<float>& a, in
 #endif
 #ifndef LBM_STEP_MIN_BLOCKS_16
 #define LBM_STEP_MIN_BLOCKS_16 3
-#endif
-#ifndef LBM_PACKED16
-#define LBM_PACKED16 1
 #endif
 #ifndef LBM_STEP_MIN_BLOCKS_16_V8
 #define LBM_STEP_MIN_BLOCKS_16_V8 2
@@ -1215,11 +1276,15 @@ lbm_step_kernel(const StepArgs<typename Store<S>::CT> a) {
     if (b < gblocks) {
         const int e = b * rows + threadIdx.y;
         if (e >= a.ngtiles) return;
-        const uint32_t t = a.gtiles[e];
+        const uint32_t entry = a.gtiles[e];
+        const uint32_t t = entry & 0x7fffffffu;
         const int y = int(t / uint32_t(a.ntiles));
         const int tile = int(t - uint32_t(y) * uint32_t(a.ntiles));
-        if constexpr (Store<S>::DEV && LBM_PACKED16) step_general_packed<S, V, FRAME, SR>(a, y, tile, threadIdx.x);
-        else step_general<S, V, FRAME, FAST, SR>(a, y, tile, threadIdx.x);
+        if (entry >> 31) {       // solids nearby, no lattice edge within reach (warp-uniform)
+            step_listed<S, V, FRAME, FAST, SR, false>(a, y, tile);
+        } else {
+            step_listed<S, V, FRAME, FAST, SR, true>(a, y, tile);
+        }
         return;
     }
     const int ib = b - gblocks;
@@ -1227,12 +1292,11 @@ lbm_step_kernel(const StepArgs<typename Store<S>::CT> a) {
     const int y = by * rows + threadIdx.y;
     if (y >= a.h) return;                                                  // warp-uniform
     if (a.tflags == nullptr) {
-        if constexpr (Store<S>::DEV && LBM_PACKED16) step_general_packed<S, V, FRAME, SR>(a, y, tile, threadIdx.x);
-        else step_general<S, V, FRAME, FAST, SR>(a, y, tile, threadIdx.x);
+        step_listed<S, V, FRAME, FAST, SR, true>(a, y, tile);
         return;
     }
     const uint8_t flag = a.tflags[int64_t(y) * a.ntiles + tile];        // warp-uniform
-    if (flag == 1) return;                                                 // owned by the list
+    if (flag & 1) return;                                                  // 1, 3: owned by the list
     const int x0 = (tile * 32 + threadIdx.x) * V;
     if constexpr (Store<S>::DEV && LBM_PACKED16) {
         if (flag == 0) step_interior_packed<S, V, FRAME, SR>(a, y, x0, threadIdx.x);
