@@ -55,6 +55,9 @@ constexpr int kBatchGraphSteps = 16;
 #ifndef LBM_BATCH_MIN_BLOCKS
 #define LBM_BATCH_MIN_BLOCKS 3
 #endif
+#ifndef LBM_BATCH_PREFETCH
+#define LBM_BATCH_PREFETCH 1
+#endif
 
 // One warp = one work item; a warp walks its item list with a stride of the
 // whole grid, fetching the next item before it works on the current one, and
@@ -75,6 +78,20 @@ lbm_batch_kernel(const lbm_batch_member_dev* __restrict__ members, const uint2* 
     uint2 item = it < nitems ? items[it] : make_uint2(0u, 0u);
     for (; it < nitems; it += warps) {
         const uint2 next = it + warps < nitems ? items[it + warps] : make_uint2(0u, 0u);
+        if (LBM_BATCH_PREFETCH && lane < 9 && it + warps < nitems) {
+            // L2 prefetch of the rows the next item pulls, one plane a lane
+            // (the range is clipped to the row's pitch, so it stays inside
+            // the member's buffer)
+            const StepArgs<float>& an = members[next.x].a[parity];
+            const int ys = int(next.y >> 12) - DROW(FRAME, lane);
+            const int x0 = int(next.y & 4095u) * 32 * V;
+            if (ys >= 0 && ys < an.h) {
+                const int n = min(32 * V, an.pitch - x0);
+                const float* p = static_cast<const float*>(an.src) + lane * an.plane +
+                                 int64_t(ys) * an.pitch + x0;
+                asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" :: "l"(p), "r"(n * 4) : "memory");
+            }
+        }
         const StepArgs<float>& a = members[item.x].a[parity];
         const int y = int(item.y >> 12), tile = int(item.y & 4095u);
         if constexpr (PATH == 1) step_general<float, V, FRAME, FAST>(a, y, tile, lane);
