@@ -10,16 +10,20 @@
 // of 128 bytes), x contiguous.  A warp owns 32*V consecutive cells of one row;
 // each lane loads V cells of a plane with one aligned vector load (16 bytes
 // for f32 V=4, f64 V=2, 16-bit V=8).  The +-1 column shifts of the pull are
-// realigned in registers with warp shuffles, so every global load is an
+// realigned in registers with warp shuffles (16-bit values stay packed two
+// per register and shift by byte permutes), so every global load is an
 // aligned, coalesced vector; only the two lanes at a warp's ends fetch one
 // extra scalar (an L1/L2 hit).  Row shifts are plain row offsets.
 //
-// Each step is one launch with two paths: the interior path for every
-// (row, warp tile) whose 3 x (32V + 2) neighbourhood is inside the lattice and
-// fluid (no boundary logic at all), and the general path, with the full
-// boundary treatment, for the listed remaining tiles (lattice edges, solids).
-// The per-tile flags and the list are rebuilt whenever the geometry or the
-// tile width changes.
+// Each step is one launch.  Per (row, warp tile) flag: 0 = the interior path
+// (the 3 x (32V + 2) neighbourhood is inside the lattice and fluid: no
+// boundary logic at all), 2 = the same with wrapped rows / columns at
+// periodic edges, 1 = the general path with the full boundary treatment
+// (non-periodic edges), 3 = the general path without edge handling (solids
+// nearby, every source cell inside the lattice).  Tiles 1 and 3 are listed
+// and run first.  Interior warps also prefetch into L2 the rows that warps
+// further down the row-major wavefront will pull.  The flags and the list
+// are rebuilt whenever the geometry or the tile width changes.
 #pragma once
 
 #include "lbm_common.cuh"
@@ -1246,12 +1250,13 @@ __device__ __forceinline__ void step_listed(const StepArgs<typename Store<S>::CT
 }
 
 // One step over the whole lattice in one launch.  With tile flags: the first
-// ceil(ngtiles / rows) blocks take the flagged tiles from the list a.gtiles
-// (entry = row * ntiles + tile), one warp per entry, so their longer latency
-// overlaps the rest; the remaining blocks cover every (row, tile) in row-major
-// order and run the interior path, leaving tiles flagged 1 to the list.
-// Without tile flags, every tile takes the general path.
-// Resident blocks of 256 threads the register allocation is sized for (V <= 4).
+// ceil(ngtiles / rows) blocks take the listed tiles from a.gtiles (entry =
+// row * ntiles + tile, bit 31 set for flag 3), one warp per entry, so their
+// longer latency overlaps the rest; the remaining blocks cover every (row,
+// tile) in row-major order and run the interior paths, leaving tiles flagged
+// 1 or 3 to the list.  Without tile flags, every tile takes the general path.
+// Resident blocks of 256 threads the register allocation is sized for: 3 at
+// 4 cells per thread (f32 and 16-bit), 2 for 16-bit at 8 cells, 1 otherwise.
 #ifndef LBM_STEP_MIN_BLOCKS
 #define LBM_STEP_MIN_BLOCKS 3
 #endif
