@@ -26,6 +26,8 @@
 // are rebuilt whenever the geometry or the tile width changes.
 #pragma once
 
+#include <array>
+
 #include "lbm_common.cuh"
 #include "lbm_pair.cuh"
 
@@ -1327,19 +1329,25 @@ void launch_step_tv(const StepArgs<typename Store<S>::CT>& a, int rows, cudaStre
     StepArgs<typename Store<S>::CT> b = a;
     b.ntiles = ntiles;
     if (b.pf_rows < 0) {
-        // resident blocks per SM of this kernel at this block size, and SMs
-        // (cached per instantiation; the same GPU model throughout)
-        static int occ[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-        static int sms = 0;
-        if (sms == 0) {
-            int dev = 0;
-            if (cudaGetDevice(&dev) == cudaSuccess)
-                cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        }
-        if (occ[rows] == 0)
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[rows], lbm_step_kernel<S, V, FRAME, FAST, SR>,
-                                                          32 * rows, 0);
-        const int64_t wave_rows = int64_t(occ[rows]) * sms * rows / ntiles;
+        // Resident blocks per SM of this kernel at each block size, times
+        // the SMs: computed once per instantiation (thread-safe static
+        // initialisation; one GPU model per process).  0 turns the prefetch off.
+        static const std::array<int, 9> blocks_per_gpu = [] {
+            std::array<int, 9> out{};
+            int dev = 0, sms = 0;
+            if (cudaGetDevice(&dev) != cudaSuccess ||
+                cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+                return out;
+            for (int r = 1; r <= 8; ++r) {
+                int occ = 0;
+                if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                        &occ, lbm_step_kernel<S, V, FRAME, FAST, SR>, 32 * r, 0) == cudaSuccess)
+                    out[r] = occ * sms;
+            }
+            (void)cudaGetLastError();
+            return out;
+        }();
+        const int64_t wave_rows = int64_t(blocks_per_gpu[rows]) * rows / ntiles;
         b.pf_rows = int(wave_rows * LBM_PREFETCH_PCT / 100);
     }
     lbm_step_kernel<S, V, FRAME, FAST, SR><<<gblocks + ntiles * rowblocks, dim3(32, rows), 0, stream>>>(b);
