@@ -453,7 +453,10 @@ __global__ void tile_flags_kernel(uint8_t* __restrict__ tflags, const uint8_t* _
         }
         // 3: solids nearby but every source cell inside the lattice (the
         // general path without edge handling); 1: the full general path
-        tflags[t] = gen ? ((solid_gen && !xedge && !yedge) ? 3 : 1) : ((xedge || yedge) ? 2 : 0);
+        // Unlisted tiles: 2 for the partial last tile of a periodic row (the
+        // wrapping path), 0 otherwise (the interior path wraps rows and its
+        // edge columns at periodic edges itself).
+        tflags[t] = gen ? ((solid_gen && !xedge && !yedge) ? 3 : 1) : ((xs + tile_w > w) ? 2 : 0);
     }
 }
 

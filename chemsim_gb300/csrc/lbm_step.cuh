@@ -16,11 +16,11 @@
 // extra scalar (an L1/L2 hit).  Row shifts are plain row offsets.
 //
 // Each step is one launch.  Per (row, warp tile) flag: 0 = the interior path
-// (the 3 x (32V + 2) neighbourhood is inside the lattice and fluid: no
-// boundary logic at all), 2 = the same with wrapped rows / columns at
-// periodic edges, 1 = the general path with the full boundary treatment
-// (non-periodic edges), 3 = the general path without edge handling (solids
-// nearby, every source cell inside the lattice).  Tiles 1 and 3 are listed
+// (the 3 x (32V + 2) neighbourhood is fluid and inside the lattice, or wraps
+// at periodic edges: no boundary logic), 2 = the same for the partial last
+// tile of a periodic row, 1 = the general path with the full boundary
+// treatment (non-periodic edges), 3 = the general path without edge handling
+// (solids nearby, every source cell inside the lattice).  Tiles 1 and 3 are listed
 // and run first.  Interior warps also prefetch into L2 the rows that warps
 // further down the row-major wavefront will pull.  The flags and the list
 // are rebuilt whenever the geometry or the tile width changes.
@@ -496,6 +496,26 @@ __device__ __forceinline__ void zero_past_edge(typename Store<S>::CT (&f)[9][V],
             if (x0 + k >= w) f[i][k] = 0;
 }
 
+// Source rows and warp-edge columns of an interior tile.  Rows wrap at the
+// y edges and columns at the x edges: an interior tile reaches an edge only
+// when that axis is periodic (tiles at other edges are listed), so the wrap
+// is always the right rule.
+struct InteriorRows {
+    int64_t rm, r0, rp;     // element offsets of rows y - 1, y, y + 1
+    int left, right;        // columns x0 - 1 and x0 + V, wrapped
+    template <class CT>
+    __device__ __forceinline__ InteriorRows(const StepArgs<CT>& a, int y, int x0, int V) {
+        const int64_t P = a.pitch;
+        rm = int64_t(y == 0 ? a.h - 1 : y - 1) * P;
+        r0 = int64_t(y) * P;
+        rp = int64_t(y == a.h - 1 ? 0 : y + 1) * P;
+        left = x0 == 0 ? a.w - 1 : x0 - 1;
+        right = x0 + V == a.w ? 0 : x0 + V;
+    }
+    // offset of the source row of a direction with row displacement dr
+    __device__ __forceinline__ int64_t of(int dr) const { return dr == 1 ? rm : (dr == -1 ? rp : r0); }
+};
+
 // Interior warp tile (flag 0): every source cell is inside the lattice and
 // fluid, so a step is 9 vector loads, 6 shuffles and two edge scalars per
 // lane, the collision and 9 vector stores.
@@ -504,18 +524,19 @@ __device__ __forceinline__ void step_interior(const StepArgs<typename Store<S>::
                                               int x0, int lane) {
     using CT = typename Store<S>::CT;
     using ST = Store<S>;
-    const S* __restrict__ base = static_cast<const S*>(a.src) + int64_t(y) * a.pitch + x0;
-    const int64_t P = a.pitch, PL = a.plane;
+    const S* __restrict__ src = static_cast<const S*>(a.src);
+    const int64_t PL = a.plane;
+    const InteriorRows rows(a, y, x0, V);
     S raw[9][V];
     S edge[9];
 #pragma unroll
     for (int i = 0; i < 9; ++i) {
         const int dc = DCOL(FRAME, i), dr = DROW(FRAME, i);
-        const S* p = base + i * PL - dr * P;
-        VecIO<S, V>::load(p, raw[i]);
+        const S* prow = src + i * PL + rows.of(dr);
+        VecIO<S, V>::load(prow + x0, raw[i]);
         edge[i] = raw[i][0];
-        if (dc == 1 && lane == 0) edge[i] = __ldg(p - 1);
-        if (dc == -1 && lane == 31) edge[i] = __ldg(p + V);
+        if (dc == 1 && lane == 0) edge[i] = __ldg(prow + rows.left);
+        if (dc == -1 && lane == 31) edge[i] = __ldg(prow + rows.right);
     }
     prefetch_ahead<S, V, FRAME>(a, y, x0, lane);
     CT f[9][V];
@@ -552,12 +573,13 @@ __device__ __forceinline__ void step_interior(const StepArgs<typename Store<S>::
 // classifies boundary links; phase C fetches the cell's own opposite
 // populations for bounce-back links (only near walls and solids); phase D
 // collides and stores.
-// Periodic-edge warp tile (flag 2): every source cell is fluid and the tile
-// reaches only periodic lattice edges.  A step is 9 vector loads, 6 shuffles, two edge
-// scalars per lane, the collision and 9 vector stores; the edge rows and
-// columns wrap.  On a partial last tile, lanes past the edge only feed the
-// shuffles, and the lane holding column w - 1 takes column 0 for the cell
-// whose source lies past the edge.
+// Periodic-edge warp tile (flag 2): the partial last tile of a row of a
+// lattice periodic in x (full tiles at periodic edges take the interior
+// path, which wraps rows and its edge columns).  Every source cell is fluid.
+// A step is 9 vector loads, 6 shuffles, two edge scalars per lane, the
+// collision and 9 vector stores; the edge rows and columns wrap.  Lanes past
+// the edge only feed the shuffles, and the lane holding column w - 1 takes
+// column 0 for the cell whose source lies past the edge.
 template <class S, int V, int FRAME, bool FAST, bool SR = false>
 __device__ __forceinline__ void step_interior_wrap(const StepArgs<typename Store<S>::CT>& a, int y,
                                               int x0, int lane) {
@@ -790,18 +812,19 @@ template <class S, int V, int FRAME, bool SR>
 __device__ __forceinline__ void step_interior_packed(const StepArgs<float>& a, int y, int x0,
                                                      int lane) {
     constexpr int NP = V / 2;
-    const S* __restrict__ base = static_cast<const S*>(a.src) + int64_t(y) * a.pitch + x0;
-    const int64_t P = a.pitch, PL = a.plane;
+    const unsigned short* __restrict__ src = static_cast<const unsigned short*>(a.src);
+    const int64_t PL = a.plane;
+    const InteriorRows rows(a, y, x0, V);
     uint32_t r[9][NP];
     uint32_t edge[9];
 #pragma unroll
     for (int i = 0; i < 9; ++i) {
         const int dc = DCOL(FRAME, i), dr = DROW(FRAME, i);
-        const S* p = base + i * PL - dr * P;
-        PackIO<NP>::load(p, r[i]);
+        const unsigned short* prow = src + i * PL + rows.of(dr);
+        PackIO<NP>::load(prow + x0, r[i]);
         edge[i] = 0u;
-        if (dc == 1 && lane == 0) edge[i] = uint32_t(__ldg(reinterpret_cast<const unsigned short*>(p - 1))) << 16;
-        if (dc == -1 && lane == 31) edge[i] = __ldg(reinterpret_cast<const unsigned short*>(p + V));
+        if (dc == 1 && lane == 0) edge[i] = uint32_t(__ldg(prow + rows.left)) << 16;
+        if (dc == -1 && lane == 31) edge[i] = __ldg(prow + rows.right);
     }
     prefetch_ahead<S, V, FRAME>(a, y, x0, lane);
 #pragma unroll

@@ -474,13 +474,15 @@ def _raw_planes(lat, path):
 @pytest.mark.parametrize("cells", [4, 8])
 @pytest.mark.parametrize("frame", [0, FRAME_XY])
 @pytest.mark.parametrize("collision", [0, COLLISION_TRT])
+@pytest.mark.parametrize("partial", [True, False])
 def test_interior_paths_match_general_path(gpu, tmp_path, precision, extra, cells, frame,
-                                           collision):
+                                           collision, partial):
     """One step from the same random state: every cell whose periodic 3 x 3
     neighbourhood holds no solid gets the same stored bits whether its warp
-    tile runs an interior path (no solids anywhere: lean and periodic-edge
-    tiles) or the general path (sparse solids flag most tiles)."""
-    w, h = 32 * cells * 3 + 37, 40          # a partial last tile
+    tile runs an interior path (no solids anywhere: the interior path, which
+    wraps at the periodic edges, and the partial last tile's path) or the
+    general path (sparse solids flag most tiles)."""
+    w, h = 32 * cells * 3 + (37 if partial else 0), 40
     flags = X_PERIODIC | Y_PERIODIC | frame | FAST | extra
     rng = np.random.default_rng(cells + 7 * frame)
     solid = np.zeros((h, w), np.uint8)
