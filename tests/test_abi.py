@@ -27,6 +27,36 @@ def test_every_header_function_has_a_signature():
     assert declared <= set(_lib.SIGNATURES), declared - set(_lib.SIGNATURES)
 
 
+def _header_arities():
+    """Parameter count of every function declared in include/*.h."""
+    import os
+    import re
+    out = {}
+    for fn in sorted(os.listdir(_lib.HEADER_DIR)):
+        if not fn.endswith(".h"):
+            continue
+        text = re.sub(r"/\*.*?\*/", "", open(os.path.join(_lib.HEADER_DIR, fn)).read(), flags=re.S)
+        for m in re.finditer(r"\b(lbm_\w+)\s*\(([^)]*)\)\s*;", text):
+            args = m.group(2).strip()
+            out[m.group(1)] = 0 if args in ("", "void") else args.count(",") + 1
+    return out
+
+
+def test_rust_binding_declares_every_entry_point():
+    """The extern block in INTEGRATION.md names every function of the header
+    with the same number of parameters, and nothing else."""
+    import os
+    import re
+    text = open(os.path.join(os.path.dirname(_lib.HEADER_DIR), "INTEGRATION.md")).read()
+    rust = {m.group(1): (0 if not m.group(2).strip() else m.group(2).count(",") + 1)
+            for m in re.finditer(r"pub fn (lbm_\w+)\(([^)]*)\)", text, re.S)}
+    header = _header_arities()
+    assert set(header) == set(_lib.header_functions())
+    assert set(rust) == set(header), (set(header) ^ set(rust))
+    wrong = {n: (header[n], rust[n]) for n in header if header[n] != rust[n]}
+    assert not wrong, wrong
+
+
 def test_version_and_error_string(cuda_lib):
     assert cuda_lib.lbm_version() >= 100
     assert isinstance(_lib.last_error(), str)
