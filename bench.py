@@ -88,7 +88,7 @@ def parse_args():
                    help="skip the 16384^2 f16 / 8192^2 f32 comparison")
     p.add_argument("--large-steps", type=int, default=500)
     p.add_argument("--no-learned", action="store_true",
-                   help="skip the learned coarse-grid correction (train + judge)")
+                   help="skip the learned coarse-grid correction (train + evaluate)")
     p.add_argument("--learned-iters", type=int, default=3000, help="Adam iterations")
     return p.parse_args()
 

@@ -420,7 +420,7 @@ def evaluate_correction(cfg: CorrectionConfig, net, s_eff: float, stream, gains=
 
 
 def run_correction_experiment(cfg: CorrectionConfig, log=None, gains=None) -> dict:
-    """Trains the correction (train_correction) and judges it on a held-out
+    """Trains the correction (train_correction) and evaluates it on a held-out
     geometry (evaluate_correction).  Returns a result dict."""
     import torch
     stream = torch.cuda.Stream()
