@@ -29,14 +29,17 @@ def slab_rows(h: int, rank: int, world: int) -> tuple[int, int]:
     return rank * h // world, (rank + 1) * h // world
 
 
-def step_slab(f_halo: np.ndarray, *, tau: float, x_flags: int, frame_xy: int) -> np.ndarray:
+def step_slab(f_halo: np.ndarray, *, tau: float, x_flags: int, frame_xy: int,
+              **step_kw) -> np.ndarray:
     """One step of a slab with its halo rows (9, rows + 2, w); returns the
-    interior rows (9, rows, w)."""
-    out = oracle.step(f_halo, 1, tau=tau, flags=x_flags | FLAG_Y_ZEROPAD | frame_xy)
+    interior rows (9, rows, w).  step_kw (force, collision, tau_minus) go to
+    the oracle's step: the body force and the collision are local to a cell."""
+    out = oracle.step(f_halo, 1, tau=tau, flags=x_flags | FLAG_Y_ZEROPAD | frame_xy, **step_kw)
     return out[:, 1:-1]
 
 
-def run_rank(f_global: np.ndarray, nsteps: int, tau: float, x_flags: int, frame_xy: int, dist):
+def run_rank(f_global: np.ndarray, nsteps: int, tau: float, x_flags: int, frame_xy: int, dist,
+             **step_kw):
     """The slab of this rank after nsteps steps, exchanging halos with its
     neighbours through `dist` (torch.distributed, any backend)."""
     import torch
@@ -60,5 +63,5 @@ def run_rank(f_global: np.ndarray, nsteps: int, tau: float, x_flags: int, frame_
             r.wait()
         halo[list(UP), 0] = recv_from_below.numpy()
         halo[list(DOWN), -1] = recv_from_above.numpy()
-        slab = step_slab(halo, tau=tau, x_flags=x_flags, frame_xy=frame_xy)
+        slab = step_slab(halo, tau=tau, x_flags=x_flags, frame_xy=frame_xy, **step_kw)
     return slab

@@ -22,20 +22,24 @@ def _free_port():
     return port
 
 
-def _rank_main(rank, world, port, f_path, out_dir, nsteps, tau):
+def _rank_main(rank, world, port, f_path, out_dir, nsteps, tau, step_kw):
     import torch.distributed as dist
     dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank,
                             world_size=world)
     try:
         f = np.load(f_path)
-        slab = halo.run_rank(f, nsteps, tau, X_PERIODIC, FRAME_XY, dist)
+        slab = halo.run_rank(f, nsteps, tau, X_PERIODIC, FRAME_XY, dist, **step_kw)
         np.save(os.path.join(out_dir, f"slab{rank}.npy"), slab)
     finally:
         dist.destroy_process_group()
 
 
-@pytest.mark.parametrize("world,h", [(2, 24), (3, 31)])
-def test_slab_partition_matches_single_domain(tmp_path, world, h):
+@pytest.mark.parametrize("world,h,step_kw", [
+    (2, 24, {}),
+    (3, 31, {}),
+    (2, 26, {"force": (2e-4, -1e-4), "collision": 1, "tau_minus": 0.9}),   # Guo force, TRT
+])
+def test_slab_partition_matches_single_domain(tmp_path, world, h, step_kw):
     oracle.build()
     rng = np.random.default_rng(world)
     w, tau, nsteps = 20, 0.7, 6
@@ -46,7 +50,7 @@ def test_slab_partition_matches_single_domain(tmp_path, world, h):
     f_path = str(tmp_path / "f.npy")
     np.save(f_path, f)
     torch.multiprocessing.spawn(_rank_main, args=(world, _free_port(), f_path, str(tmp_path),
-                                                  nsteps, tau), nprocs=world, join=True)
+                                                  nsteps, tau, step_kw), nprocs=world, join=True)
     got = np.concatenate([np.load(tmp_path / f"slab{r}.npy") for r in range(world)], axis=1)
-    ref = oracle.step(f, nsteps, tau=tau, flags=X_PERIODIC | Y_PERIODIC | FRAME_XY)
+    ref = oracle.step(f, nsteps, tau=tau, flags=X_PERIODIC | Y_PERIODIC | FRAME_XY, **step_kw)
     assert np.array_equal(got, ref)
