@@ -39,14 +39,19 @@ def step_slab(f_halo: np.ndarray, *, tau: float, x_flags: int, frame_xy: int,
 
 
 def run_rank(f_global: np.ndarray, nsteps: int, tau: float, x_flags: int, frame_xy: int, dist,
-             **step_kw):
+             solid=None, **step_kw):
     """The slab of this rank after nsteps steps, exchanging halos with its
-    neighbours through `dist` (torch.distributed, any backend)."""
+    neighbours through `dist` (torch.distributed, any backend).  A solid mask
+    (h, w) is static, so every rank cuts its slab's rows and the two halo
+    rows from it without an exchange."""
     import torch
     rank, world = dist.get_rank(), dist.get_world_size()
     _, h, w = f_global.shape
     y0, y1 = slab_rows(h, rank, world)
     slab = np.ascontiguousarray(f_global[:, y0:y1])
+    if solid is not None:
+        rows = [(y0 - 1) % h] + list(range(y0, y1)) + [y1 % h]
+        step_kw = dict(step_kw, solid=np.ascontiguousarray(np.asarray(solid)[rows]))
     above, below = (rank + 1) % world, (rank - 1) % world
     for _ in range(nsteps):
         halo = np.zeros((9, slab.shape[1] + 2, w), dtype=slab.dtype)
