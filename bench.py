@@ -67,7 +67,9 @@ sys.path.insert(0, ROOT)
 BYTES_F32 = 72          # 9 loads + 9 stores x 4 B
 BYTES_F16 = 36
 BYTES_MASK = 1          # u8 solid mask read once per cell
-WORKLOAD = "channel_4096x4096_tau0.56_walls_y_periodic_x_force1e-6_64obstacles_r16-64"
+def workload_name(n: int) -> str:
+    """The headline workload at side n (channel_spec(n): 64 obstacles at every size)."""
+    return f"channel_{n}x{n}_tau0.56_walls_y_periodic_x_force1e-6_64obstacles_r16-64"
 
 
 def parse_args():
@@ -274,7 +276,7 @@ def run_reference(args):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": secs / args.steps * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "sample_rows": spec.h, "parallelism": "cpu"},
+        "config": {"workload": workload_name(args.size), "sample_rows": spec.h, "parallelism": "cpu"},
         "cpu_baseline": {"value": round(mlups, 3), "unit": "MLUPS", "cores": threads,
                          "kind": "port", "sample": sample},
         "e2e": {"value": round(mlups, 3), "unit": "MLUPS", "h2d_bytes_per_step": 0,
@@ -408,9 +410,11 @@ def run_ours(args):
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(step_s * 1e3, 5), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "cells": cells,
+            "config": {"workload": workload_name(args.size), "cells": cells,
                        "arithmetic": "reference order" if args.strict else "LBM_FAST (FMA)",
-                       "l2": "inputs larger than L2 (1.2 GB of populations per step); no flush",
+                       "l2": (f"inputs larger than L2 ({72 * cells / 1e9:.1f} GB of populations per "
+                              "step); no flush") if 72 * cells > 129e6 else
+                             "inputs smaller than L2: no flush, the roofline fraction is not an HBM figure",
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "hbm_gbs": round(achieved, 1),
             "roofline": roofline,

@@ -1,0 +1,29 @@
+"""bench.py's reference arm prints the JSON line of the benchmark contract
+(CPU only: the arm times the oracle's restatement of the reference step)."""
+import json
+import os
+import subprocess
+import sys
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_reference_arm_json_line():
+    out = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--size", "256",
+                          "--steps", "3", "--warmup", "3"],
+                         cwd=ROOT, capture_output=True, text=True, timeout=600, check=True)
+    line = json.loads(out.stdout.strip().splitlines()[-1])
+    for key in ("metric", "value", "unit", "impl", "n_gpus", "steps", "warmup", "ms_per_step",
+                "higher_is_better", "scaling", "vs_baseline", "dtype", "data", "config",
+                "cpu_baseline", "e2e"):
+        assert key in line, key
+    assert line["impl"] == "reference" and line["metric"] == "D2Q9 MLUPS"
+    assert line["unit"] == "MLUPS" and line["higher_is_better"] is True
+    assert line["steps"] == 3 and line["warmup"] == 3 and line["n_gpus"] == 1
+    assert line["value"] > 0 and line["ms_per_step"] > 0
+    assert line["config"]["workload"].startswith("channel_256x256_")
+    cb = line["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == line["value"]
+    e2e = line["e2e"]
+    assert e2e["value"] == line["value"] and e2e["h2d_bytes_per_step"] == 0
+    assert e2e["d2h_bytes_per_step"] == 0
