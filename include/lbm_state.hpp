@@ -9,8 +9,8 @@
 //   BGK, TRT                  src/lbm.rs:345-451
 //   State<L>::initial / step / size / delta_x / delta_t / populations /
 //   isothermal_speed_of_sound / density / pressure / momentum_density /
-//   velocity / speed / equilibrium / non_equilibrium / is_unstable
-//                             src/lbm.rs:670-819
+//   velocity / speed / equilibrium / non_equilibrium / is_unstable /
+//   geometry               src/lbm.rs:670-819
 // Fields are row-major y * w + x vectors (the layout of Matrix::new /
 // get_underlying); populations are 9 such planes in D2Q9 direction order.
 // Where lbm.rs panics (assert!), this header throws std::logic_error; a
@@ -239,31 +239,39 @@ class State {
     }
     const Lattice& device() const { return lat_; }
 
+    // State::geometry, a pub field (src/lbm.rs:670-676) that LBMSim::handle
+    // reads and replaces between steps (src/main.rs:77-89): w * h booleans,
+    // true = solid, or empty for none.
+    const std::vector<bool>& geometry() const { return geometry_; }
+    void set_geometry(std::vector<bool> g) {
+        require(g.empty() || g.size() == lat_.cells(), "geometry size");
+        std::vector<uint8_t> m(g.begin(), g.end());
+        check(lbm_set_geometry(lat_.raw(), g.empty() ? nullptr : m.data()));
+        geometry_ = std::move(g);
+    }
+
     Discretization discretization;
 
   private:
     State(const D2Q9& lattice, std::vector<bool> geometry, const BGK& c, const Discretization& d,
           int precision, int flags)
         : discretization(d), lat_(lattice.size().first, lattice.size().second, c.tau, precision, flags) {
-        setup(lattice, geometry);
+        setup(lattice, std::move(geometry));
     }
     State(const D2Q9& lattice, std::vector<bool> geometry, const TRT& c, const Discretization& d,
           int precision, int flags)
         : discretization(d),
           lat_(lattice.size().first, lattice.size().second, c.tau_plus, precision, flags) {
         check(lbm_set_collision(lat_.raw(), LBM_COLLISION_TRT, c.tau_plus, c.tau_minus));
-        setup(lattice, geometry);
+        setup(lattice, std::move(geometry));
     }
-    void setup(const D2Q9& lattice, const std::vector<bool>& geometry) {
+    void setup(const D2Q9& lattice, std::vector<bool> geometry) {
         check(lbm_set_discretization(lat_.raw(), discretization.delta_x, discretization.delta_t));
         lat_.set_populations(lattice.pops);
-        if (!geometry.empty()) {
-            require(geometry.size() == lat_.cells(), "geometry size");
-            std::vector<uint8_t> g(geometry.begin(), geometry.end());
-            check(lbm_set_geometry(lat_.raw(), g.data()));
-        }
+        if (!geometry.empty()) set_geometry(std::move(geometry));
     }
     Lattice lat_;
+    std::vector<bool> geometry_;
 };
 
 }  // namespace chemsim
