@@ -1,5 +1,6 @@
 """The C-ABI library builds, loads and exports its header; host-side logic (CPU)."""
 import ctypes
+import os
 import subprocess
 
 import numpy as np
@@ -42,19 +43,73 @@ def _header_arities():
     return out
 
 
+CRATE = os.path.join(os.path.dirname(_lib.HEADER_DIR), "lbm-cuda")
+
+
 def test_rust_binding_declares_every_entry_point():
-    """The extern block in INTEGRATION.md names every function of the header
-    with the same number of parameters, and nothing else."""
-    import os
+    """The extern block of the lbm-cuda crate (lbm-cuda/src/lib.rs) names
+    every function of the header with the same number of parameters, and
+    nothing else."""
     import re
-    text = open(os.path.join(os.path.dirname(_lib.HEADER_DIR), "INTEGRATION.md")).read()
+    text = open(os.path.join(CRATE, "src", "lib.rs")).read()
+    block = text[text.index('extern "C" {'):]
+    block = block[:block.index("\n    }\n")]
     rust = {m.group(1): (0 if not m.group(2).strip() else m.group(2).count(",") + 1)
-            for m in re.finditer(r"pub fn (lbm_\w+)\(([^)]*)\)", text, re.S)}
+            for m in re.finditer(r"pub fn (lbm_\w+)\(([^)]*)\)", block, re.S)}
     header = _header_arities()
     assert set(header) == set(_lib.header_functions())
     assert set(rust) == set(header), (set(header) ^ set(rust))
     wrong = {n: (header[n], rust[n]) for n in header if header[n] != rust[n]}
     assert not wrong, wrong
+
+
+def test_rust_structs_and_constants_match_the_header():
+    """lbm_health / lbm_desc field order and the LBM_* constants of the
+    crate are those of include/lbm_cuda.h."""
+    import re
+    header = re.sub(r"/\*.*?\*/", "", open(os.path.join(_lib.HEADER_DIR, "lbm_cuda.h")).read(),
+                    flags=re.S)
+    rust = open(os.path.join(CRATE, "src", "lib.rs")).read()
+    for cname, rname in (("lbm_health", "LbmHealth"), ("lbm_desc", "LbmDesc")):
+        body = re.search(r"typedef struct %s \{(.*?)\}" % cname, header, re.S).group(1)
+        cfields = re.findall(r"(\w+)\s*(?:,|;)", body.replace("*", " "))
+        rbody = re.search(r"pub struct %s \{(.*?)\}" % rname, rust, re.S).group(1)
+        rfields = re.findall(r"pub (\w+):", rbody)
+        assert cfields == rfields, (cname, cfields, rfields)
+    consts = dict(re.findall(r"#define (LBM_\w+)\s+\(?(-?(?:0x)?[0-9a-fA-F]+)\)?", header))
+    rconsts = dict(re.findall(r"pub const (LBM_\w+): c_int = (-?(?:0x)?[0-9a-fA-F]+);", rust))
+    assert rconsts, "no constants in the crate"
+    for name, val in rconsts.items():
+        assert int(consts[name], 0) == int(val, 0), name
+    missing = {n for n in consts if n.startswith(("LBM_ERR", "LBM_F", "LBM_X", "LBM_Y", "LBM_COLL",
+                                                 "LBM_RENDER", "LBM_SOLID"))} - set(rconsts)
+    assert not missing, missing
+
+
+def test_rust_build_script_and_chemsim_patch():
+    """build.rs compiles the library's own CUDA sources for sm_103a (or links
+    the prebuilt .so); chemsim.patch is a unified diff against chemsim that
+    routes State's step, moments and health through the crate."""
+    build = open(os.path.join(CRATE, "build.rs")).read()
+    assert "arch=compute_103a,code=sm_103a" in build and ".cuda(true)" in build
+    assert "LBM_CUDA_DIR" in build and '"cu"' in build
+    cargo = open(os.path.join(CRATE, "Cargo.toml")).read()
+    assert 'name = "lbm-cuda"' in cargo and "cc =" in cargo
+    patch = open(os.path.join(CRATE, "chemsim.patch")).read()
+    files = [l.split()[1] for l in patch.splitlines() if l.startswith("+++ ")]
+    assert files == ["b/Cargo.toml", "b/src/lbm.rs", "b/src/lib.rs", "b/src/main.rs"]
+    added = "\n".join(l[1:] for l in patch.splitlines() if l.startswith("+") and not l.startswith("+++"))
+    for needle in ("dev.step(1)", "dev.moments()", "dev.health()", "fn initial_device",
+                   "fn set_geometry", "extern crate lbm_cuda", "State::initial_device"):
+        assert needle in added, needle
+    # every hunk header's line counts agree with its body
+    import re
+    for m in re.finditer(r"^@@ -\d+,(\d+) \+\d+,(\d+) @@.*?\n(.*?)(?=^@@|^diff |\Z)", patch,
+                         re.S | re.M):
+        body = m.group(3).splitlines()
+        old = sum(1 for l in body if l[:1] in (" ", "-"))
+        new = sum(1 for l in body if l[:1] in (" ", "+"))
+        assert (old, new) == (int(m.group(1)), int(m.group(2))), m.group(0)[:80]
 
 
 def test_version_and_error_string(cuda_lib):
