@@ -22,9 +22,11 @@ populations per step) are larger than L2, so no L2 flush is needed.
           finished RGBA8 frame of lbm_render_async (render.rs's colour map).
   fp16    the same lattice with half-precision deviation storage: the default
           stochastic rounding, and round_nearest (LBM_ROUND_NEAREST).
-  accuracy  rho/u L2 errors of the f32/f16/bf16 runs against the f64 run of
-          the same kernel after the same W + K steps, and the same on the
-          laminar 1024^2 Taylor-Green vortex (taylor_green_1024).
+  accuracy  rho/u L2 errors of f32/f16/bf16 storage against the f64 run of
+          the same kernel on the headline channel after --accuracy-steps
+          steps (default 5000, the channel configuration's run length,
+          whatever K is), and the same on the laminar 1024^2 Taylor-Green
+          vortex (taylor_green_1024).
   taylor_green_256  the 256^2 periodic Taylor-Green lattice (tau 0.8, 1000
           steps; L2-resident): GPU MLUPS in both arithmetics and both CPU
           steppers on the host cores.
@@ -72,6 +74,16 @@ def workload_name(n: int) -> str:
     return f"channel_{n}x{n}_tau0.56_walls_y_periodic_x_force1e-6_64obstacles_r16-64"
 
 
+def bench_config(args, world: int) -> dict:
+    """The workload both arms report (the same dict, so they compare)."""
+    cells = args.size * args.size
+    return {"workload": workload_name(args.size), "cells": cells,
+            "l2": (f"inputs larger than L2 ({72 * cells / 1e9:.1f} GB of populations per "
+                   "step); no flush") if 72 * cells > 129e6 else
+                  "inputs smaller than L2: no flush, the roofline fraction is not an HBM figure",
+            "parallelism": "replicas" if world > 1 else "single GPU"}
+
+
 def parse_args():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
@@ -81,6 +93,8 @@ def parse_args():
     p.add_argument("--size", type=int, default=4096)
     p.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     p.add_argument("--no-accuracy", action="store_true")
+    p.add_argument("--accuracy-steps", type=int, default=5000,
+                   help="steps of the accuracy leg (the channel configuration's 5000 by default)")
     p.add_argument("--strict", action="store_true",
                    help="time the reference operation order instead of LBM_FAST")
     p.add_argument("--no-batch", action="store_true", help="skip the 512-lattice batch")
@@ -276,7 +290,8 @@ def run_reference(args):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": secs / args.steps * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": workload_name(args.size), "sample_rows": spec.h, "parallelism": "cpu"},
+        "config": bench_config(args, world),
+        "arithmetic": "reference order (the op-by-op stepper)",
         "cpu_baseline": {"value": round(mlups, 3), "unit": "MLUPS", "cores": threads,
                          "kind": "port", "sample": sample},
         "e2e": {"value": round(mlups, 3), "unit": "MLUPS", "h2d_bytes_per_step": 0,
@@ -338,34 +353,13 @@ def run_ours(args):
     mlups16 = cells * args.steps / t16 / 1e6 * world
     mlups16n = cells * args.steps / t16n / 1e6 * world
 
-    accuracy = None
-    if not args.no_accuracy:
-        m32 = lat32.moments()
-        m16 = lat16.moments()
-        m16n = lat16n.moments()
-        latb = make_lattice(spec, lbm.BF16DEV, base_flags)
-        latb.step(args.warmup + args.steps)
-        mb = latb.moments()
-        latb.close()
-        lat64 = make_lattice(spec, lbm.F64, base_flags)
-        lat64.step(args.warmup + args.steps)
-        m64 = lat64.moments()
-        lat64.close()
-        fluid = spec.solid == 0
-
-        def errs(m):
-            return {"rho_dev_l2": l2_rel(m[0][fluid] - 1.0, m64[0][fluid] - 1.0),
-                    "rho_l2": l2_rel(m[0][fluid], m64[0][fluid]),
-                    "u_l2": l2_rel(np.stack([m[1][fluid], m[2][fluid]]),
-                                   np.stack([m64[1][fluid], m64[2][fluid]]))}
-        accuracy = {"steps": args.warmup + args.steps, "against": "f64 run of the same kernel",
-                    "f32": errs(m32), "f16dev": errs(m16), "f16dev_round_nearest": errs(m16n),
-                    "bf16dev": errs(mb),
-                    "u_rms_f64": float(np.sqrt(np.mean(m64[1][fluid] ** 2 + m64[2][fluid] ** 2))),
-                    "taylor_green_1024": accuracy_taylor_green(args.warmup + args.steps)}
     lat32.close()
     lat16.close()
     lat16n.close()
+    accuracy = None
+    if not args.no_accuracy and rank == 0:
+        accuracy = accuracy_channel(spec, base_flags, args.accuracy_steps)
+        accuracy["taylor_green_1024"] = accuracy_taylor_green(args.accuracy_steps)
 
     # e2e through the C ABI with pinned host buffers
     e2e = run_e2e(spec, args, torch, dist)
@@ -410,12 +404,8 @@ def run_ours(args):
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(step_s * 1e3, 5), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": workload_name(args.size), "cells": cells,
-                       "arithmetic": "reference order" if args.strict else "LBM_FAST (FMA)",
-                       "l2": (f"inputs larger than L2 ({72 * cells / 1e9:.1f} GB of populations per "
-                              "step); no flush") if 72 * cells > 129e6 else
-                             "inputs smaller than L2: no flush, the roofline fraction is not an HBM figure",
-                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "config": bench_config(args, world),
+            "arithmetic": "reference order" if args.strict else "LBM_FAST (FMA)",
             "hbm_gbs": round(achieved, 1),
             "roofline": roofline,
             "fp16": fp16,
@@ -456,6 +446,37 @@ def run_config1(torch):
     out["cpu_structured_mlups"] = round(cpu_sample(spec, 50, threads, structured=True)[0], 2)
     out["cpu_fused_mlups"] = round(cpu_sample(spec, 200, threads, structured=False)[0], 2)
     out["cpu_sample"] = "50 (structured) and 200 (fused) time steps of the same lattice"
+    return out
+
+
+def accuracy_channel(spec, flags, steps):
+    """rho/u L2 errors of f32, f16-deviation (both roundings) and
+    bf16-deviation storage against the f64 run of the same kernel on the
+    headline channel, each lattice run from the same initial state for
+    `steps` steps (the channel configuration's run length by default,
+    independent of the timed step count)."""
+    from chemsim_gb300 import lbm
+    runs = {}
+    for name, prec, extra in (("f64", lbm.F64, 0), ("f32", lbm.F32, 0), ("f16dev", lbm.F16DEV, 0),
+                              ("f16dev_round_nearest", lbm.F16DEV, lbm.ROUND_NEAREST),
+                              ("bf16dev", lbm.BF16DEV, 0)):
+        lat = make_lattice(spec, prec, flags | extra)
+        lat.step(steps)
+        runs[name] = lat.moments()
+        lat.close()
+    m64 = runs["f64"]
+    fluid = spec.solid == 0
+
+    def errs(m):
+        return {"rho_dev_l2": l2_rel(m[0][fluid] - 1.0, m64[0][fluid] - 1.0),
+                "rho_l2": l2_rel(m[0][fluid], m64[0][fluid]),
+                "u_l2": l2_rel(np.stack([m[1][fluid], m[2][fluid]]),
+                               np.stack([m64[1][fluid], m64[2][fluid]]))}
+    out = {"workload": f"{spec.w}x{spec.h} channel (the timed lattice)", "steps": steps,
+           "against": "f64 run of the same kernel"}
+    for name in ("f32", "f16dev", "f16dev_round_nearest", "bf16dev"):
+        out[name] = errs(runs[name])
+    out["u_rms_f64"] = float(np.sqrt(np.mean(m64[1][fluid] ** 2 + m64[2][fluid] ** 2)))
     return out
 
 

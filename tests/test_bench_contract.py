@@ -22,6 +22,11 @@ def test_reference_arm_json_line():
     assert line["steps"] == 3 and line["warmup"] == 3 and line["n_gpus"] == 1
     assert line["value"] > 0 and line["ms_per_step"] > 0
     assert line["config"]["workload"].startswith("channel_256x256_")
+    # the same config dict as the GPU arm's line, so the two arms compare
+    sys.path.insert(0, ROOT)
+    import argparse
+    import bench
+    assert line["config"] == bench.bench_config(argparse.Namespace(size=256), 1)
     cb = line["cpu_baseline"]
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == line["value"]
     e2e = line["e2e"]
