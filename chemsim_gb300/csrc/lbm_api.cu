@@ -883,11 +883,23 @@ int lbm_load(lbm_lattice* L, const char* path) {
     }
     std::fclose(fp);
     if (!ok) return fail(LBM_ERR_INVALID_ARGUMENT, "not a lattice checkpoint (or truncated)");
+    // Every header value is checked before the lattice changes, so a file
+    // that fails leaves the lattice as it was.
+    const bool trt = hd.collision == LBM_COLLISION_TRT;
+    if (!(hd.dx > 0.f) || !(hd.dt > 0.f) || !std::isfinite(hd.dx) || !std::isfinite(hd.dt) ||
+        (hd.collision != LBM_COLLISION_BGK && !trt) || !(hd.tau > 0.f) || !std::isfinite(hd.tau) ||
+        (trt && (!(hd.tau_minus > 0.f) || !std::isfinite(hd.tau_minus))) ||
+        !std::isfinite(hd.fx) || !std::isfinite(hd.fy) || !std::isfinite(hd.time) || hd.steps < 0)
+        return fail(LBM_ERR_INVALID_ARGUMENT,
+                    "checkpoint header holds an invalid discretization, collision, force, time or "
+                    "step count; the lattice is unchanged");
     DeviceGuard g(L->dev);
-    if (int rc = lbm_set_discretization(L, hd.dx, hd.dt)) return rc;
-    if (int rc = lbm_set_collision(L, hd.collision, hd.tau, hd.tau_minus)) return rc;
-    if (int rc = lbm_set_force(L, hd.fx, hd.fy)) return rc;
+    // The geometry upload is the one step that can still fail (device
+    // memory); it goes first, and the setters below cannot fail.
     if (int rc = lbm_set_geometry(L, hd.has_solid ? host.data() + 9 * n : nullptr)) return rc;
+    (void)lbm_set_discretization(L, hd.dx, hd.dt);
+    (void)lbm_set_collision(L, hd.collision, hd.tau, hd.tau_minus);
+    (void)lbm_set_force(L, hd.fx, hd.fy);
     for (int i = 0; i < 9; ++i)
         LBM_CUDA(cudaMemcpy2DAsync(static_cast<uint8_t*>(L->buf[L->cur]) + size_t(i) * L->plane * L->esize,
                                    size_t(L->pitch) * L->esize, host.data() + i * n, row, row, L->h,

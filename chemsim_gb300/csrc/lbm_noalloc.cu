@@ -16,6 +16,8 @@
 // exits.  One block reduces kNoAllocCellsPerBlock cells, so the largest
 // lattice is kNoAllocMaxBlocks * kNoAllocCellsPerBlock = 2^28 cells
 // (16384 x 16384); larger lattices are rejected.
+#include <cuda.h>
+
 #include <cmath>
 #include <mutex>
 #include <string>
@@ -28,14 +30,52 @@ namespace {
 
 constexpr int kNoAllocMaxBlocks = 16384;
 constexpr int64_t kNoAllocCellsPerBlock = 16384;
-constexpr int kNoAllocMaxDevices = 64;
+constexpr int kNoAllocSlots = 64;
 
 // Partials [0, kNoAllocMaxBlocks) and the result at index kNoAllocMaxBlocks.
 static __device__ __align__(256) HealthPartial g_noalloc_scratch[kNoAllocMaxBlocks + 1];
 
-// Device address of g_noalloc_scratch, resolved once per device.
+// Device address of g_noalloc_scratch, resolved once per CUDA context and
+// kept under the context's ID.  A context ID is never reused within a
+// process, so a context that replaces another (the new primary context after
+// cudaDeviceReset, whose module copy may sit elsewhere) or a second context
+// on the same device never finds another context's address.
+struct ScratchSlot {
+    unsigned long long ctx_id;
+    HealthPartial* ptr;
+};
 std::mutex g_noalloc_mutex;
-HealthPartial* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+ScratchSlot g_noalloc_slots[kNoAllocSlots] = {};
+int g_noalloc_next = 0;
+
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+
+// ID of the calling thread's current context (0 when none is current or the
+// driver entry points are unavailable; the address is then resolved afresh).
+unsigned long long current_ctx_id() {
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess && q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<CtxGetCurrentFn>(f);
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess && q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<CtxGetIdFn>(f);
+        (void)cudaGetLastError();
+    });
+    if (!get_current || !get_id) return 0;
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (get_current(&ctx) != CUDA_SUCCESS || ctx == nullptr || get_id(ctx, &id) != CUDA_SUCCESS)
+        return 0;
+    return id;
+}
 
 
 // Final reduction of the partials by one block of 256 threads: thread t sums
@@ -131,14 +171,18 @@ int lbm_check_device_noalloc(const void* populations, int precision, int w, int 
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return noalloc_fail(LBM_ERR_CUDA, cudaGetErrorString(e));
-    if (dev < 0 || dev >= kNoAllocMaxDevices)
-        return noalloc_fail(LBM_ERR_NOT_SUPPORTED, "device index beyond 63");
     HealthPartial* scratch = nullptr;
     {
-        // Set-up, once per device, with that device current: the host-side
+        // Set-up, once per context, with the device current: the host-side
         // name g_noalloc_scratch is not a device address; ask the runtime.
+        // Before the runtime's first call on this thread no context may be
+        // current (ID 0); cudaGetSymbolAddress then makes the device's
+        // primary context current, and its ID is read afterwards.
+        unsigned long long id = current_ctx_id();
         std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-        if (!g_noalloc_ptr[dev]) {
+        for (const ScratchSlot& slot : g_noalloc_slots)
+            if (id != 0 && slot.ctx_id == id) scratch = slot.ptr;
+        if (!scratch) {
             void* p = nullptr;
             e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
             if (e != cudaSuccess) {
@@ -146,9 +190,13 @@ int lbm_check_device_noalloc(const void* populations, int precision, int w, int 
                 return noalloc_fail(LBM_ERR_CUDA,
                                     std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
             }
-            g_noalloc_ptr[dev] = static_cast<HealthPartial*>(p);
+            scratch = static_cast<HealthPartial*>(p);
+            if (id == 0) id = current_ctx_id();
+            if (id != 0) {
+                g_noalloc_slots[g_noalloc_next] = ScratchSlot{id, scratch};
+                g_noalloc_next = (g_noalloc_next + 1) % kNoAllocSlots;
+            }
         }
-        scratch = g_noalloc_ptr[dev];
     }
     const int nblocks = int((cells + kNoAllocCellsPerBlock - 1) / kNoAllocCellsPerBlock);
     cudaStream_t s = static_cast<cudaStream_t>(stream);

@@ -3,8 +3,8 @@
  *
  * This is the drop-in boundary for taktoa/chemsim's `src/lbm.rs` lattice
  * storage and `State::step`.  Every entry point is plain C: opaque handles,
- * plain pointers and sizes, `int` status codes.  A Rust `lbm-cuda` crate binds
- * these with `extern "C"` declarations (the binding is in INTEGRATION.md).
+ * plain pointers and sizes, `int` status codes.  The Rust `lbm-cuda` crate
+ * (lbm-cuda/src/lib.rs) binds these with `extern "C"` declarations.
  *
  * Conventions
  *  - Status: 0 = LBM_OK, negative = LBM_ERR_*.  The message of the last error
@@ -197,8 +197,10 @@ int lbm_device_populations(lbm_lattice* lat, void** base, int64_t* plane_stride,
  * Allocates nothing: its scratch is a static 768 KiB device array that every
  * GPU loading this library holds until exit.  At most 268435456 cells
  * (16384 x 16384); larger lattices return LBM_ERR_INVALID_ARGUMENT.  The
- * first call on a device resolves the array's device address (make that
- * first call before any stream capture).  Calls share the array, so calls
+ * first call in each CUDA context (a device's primary context, the new one
+ * that follows cudaDeviceReset, or a context the caller made current)
+ * resolves the array's device address in that context (make that first call
+ * before any stream capture).  Calls share the array, so calls
  * that overlap on the GPU race; every call overwrites all of the scratch it
  * reads, so nothing needs clearing between calls.  Synchronises `stream`;
  * out->steps is 0.                                                          */

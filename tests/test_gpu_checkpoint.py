@@ -51,3 +51,35 @@ def test_load_rejects_mismatches(gpu, tmp_path):
     (tmp_path / "short.lbm").write_bytes(path.read_bytes()[:500])
     with Lattice(128, 64, 0.6, F32, FLAGS) as b, pytest.raises(lbm.LBMError):
         b.load(tmp_path / "short.lbm")                  # truncated
+
+
+# offsets of header fields (the 96-byte checkpoint header of lbm_save)
+_OFF = {"collision": 28, "tau": 40, "tau_minus": 44, "dx": 48, "dt": 52, "fx": 56, "time": 64,
+        "steps": 72}
+
+
+@pytest.mark.parametrize("field,value", [("tau", -1.0), ("dt", 0.0), ("fx", float("nan")),
+                                         ("dx", float("inf")), ("collision", 7), ("steps", -3)])
+def test_load_of_a_corrupt_header_leaves_the_lattice_unchanged(gpu, tmp_path, field, value):
+    """A header value that a setter would reject fails the load before the
+    lattice changes: populations, time, step count and the step rule stay."""
+    import struct
+    spec = channel_spec(128, n_obstacles=2, r_lo=4, r_hi=8, force=1e-5, seed=9, h=64)
+    path = tmp_path / "state.lbm"
+    with _lattice(spec, F32) as a:
+        a.step(5)
+        a.save(path)
+    raw = bytearray(path.read_bytes())
+    fmt = {"collision": "<i", "steps": "<q"}.get(field, "<f")
+    struct.pack_into(fmt, raw, _OFF[field], value)
+    (tmp_path / "bad.lbm").write_bytes(bytes(raw))
+    other = channel_spec(128, n_obstacles=3, r_lo=4, r_hi=8, force=2e-5, seed=10, h=64)
+    with _lattice(other, F32) as b, _lattice(other, F32) as ref:
+        b.step(3)
+        ref.step(3)
+        with pytest.raises(lbm.LBMError):
+            b.load(tmp_path / "bad.lbm")
+        assert b.time() == ref.time()
+        b.step(4)
+        ref.step(4)
+        assert np.array_equal(b.get_populations(), ref.get_populations())

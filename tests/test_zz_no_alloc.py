@@ -105,3 +105,28 @@ def test_noalloc_rejects_oversize_and_bad_arguments(gpu):
     rc = lib.lbm_check_device_noalloc(None, F32, 8, 8, 8, 64, 1.0, 1.0, None, ctypes.byref(out))
     assert rc == _lib.LBM_ERR_INVALID_ARGUMENT
     assert 16384 * 16384 == MAX_CELLS
+
+
+@pytest.mark.parametrize("dx,dt", [(0.25, 1.0), (1.0, 0.5), (2.0, 1.5)])
+def test_noalloc_with_discretization_and_solids(gpu, dx, dt):
+    """delta_x and delta_t set the speed of sound, which sets min f_eq[0]
+    and with it the unstable flag: the caller passes the lattice's own
+    values and gets lbm_check's answer, on a lattice with solid cells."""
+    lib = _lib.load()
+    w, h = 96, 40
+    rng = np.random.default_rng(7)
+    rho = (1 + rng.uniform(-0.01, 0.01, (h, w))).astype(np.float32)
+    ux = rng.uniform(-0.25, 0.25, (h, w)).astype(np.float32)
+    uy = rng.uniform(-0.25, 0.25, (h, w)).astype(np.float32)
+    solid = (rng.uniform(size=(h, w)) < 0.1).astype(np.uint8)
+    with Lattice(w, h, 0.8, F32, X_PERIODIC | Y_PERIODIC) as lat:
+        lat.set_discretization(dx, dt)
+        lat.set_geometry(solid)
+        lat.init_equilibrium(rho, ux, uy)
+        lat.step(2)
+        ref = lat.health()
+        for _ in range(2):
+            _agree(_noalloc(lib, lat, dx, dt), ref)
+        # the unit discretization gives a different min f_eq[0] on this state
+        unit = _noalloc(lib, lat, 1.0, 1.0)
+    assert unit["min_eq0"] != ref["min_eq0"]
