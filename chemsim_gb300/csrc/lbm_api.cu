@@ -131,6 +131,7 @@ Consts<CT> make_consts(const lbm_lattice* L) {
     for (int i = 0; i < 9; ++i) c.sgw[i] = c.dscale * c.gw[i];
     c.shfx = c.dscale * c.hfx;
     c.shfy = c.dscale * c.hfy;
+    fill_pair_consts(c);
     return c;
 }
 
@@ -186,6 +187,9 @@ int ensure_staging(lbm_lattice* L, size_t bytes) {
     return LBM_OK;
 }
 
+#ifndef LBM_LINKS_IN_GRID
+#define LBM_LINKS_IN_GRID 1
+#endif
 // Recomputes the per-(row, warp tile) boundary/solid flags for the current
 // tile width and geometry.
 int refresh_tiles(lbm_lattice* L) {
@@ -205,13 +209,33 @@ int refresh_tiles(lbm_lattice* L) {
     LBM_CUDA(cudaMemcpyAsync(flags.data(), L->tflags, flags.size(), cudaMemcpyDeviceToHost,
                              L->stream));
     LBM_CUDA(cudaStreamSynchronize(L->stream));
+    // 16-bit storage at 8 cells per thread: tiles flagged 3 take the interior
+    // path with per-lane link masks (computed here), so only tiles flagged 1
+    // are listed.
+    const bool in_grid = LBM_LINKS_IN_GRID && L->has_solid && L->vcells == 8 &&
+                         (L->precision == LBM_F16DEV || L->precision == LBM_BF16DEV);
+    if (in_grid) {
+        const size_t need = size_t(n) * 32;
+        if (need > L->links_cap) {
+            if (L->links) cudaFree(L->links);
+            L->links = nullptr;
+            L->links_cap = 0;
+            LBM_CUDA(cudaMalloc(reinterpret_cast<void**>(&L->links), need * sizeof(uint4)));
+            L->links_cap = need;
+        }
+        link_masks_kernel<<<grid_for(int64_t(need), 256), 256, 0, L->stream>>>(
+            L->links, L->tflags, L->solid, L->mpitch, L->ntiles, L->h, L->vcells,
+            (L->flags & LBM_FRAME_XY) ? 1 : 0, (L->flags & LBM_SOLID_HALFWAY) ? 1 : 0);
+        LBM_CUDA(cudaGetLastError());
+    }
+    L->use_links = in_grid;
     // Entries of tiles flagged 3 carry bit 31 (the general path without edge
     // handling); row * ntiles + tile stays below 2^31 (h <= 65535 * 8 rows).
     std::vector<uint32_t> list;
     for (int64_t t = 0; t < n; ++t) {
         const uint8_t f = flags[size_t(t)];
         if (f == 1) list.push_back(uint32_t(t));
-        else if (f == 3) list.push_back(uint32_t(t) | 0x80000000u);
+        else if (f == 3 && !in_grid) list.push_back(uint32_t(t) | 0x80000000u);
     }
     if (list.size() > L->gtiles_cap) {
         if (L->gtiles) cudaFree(L->gtiles);
@@ -382,6 +406,7 @@ StepArgs<typename Store<S>::CT> lattice_args(const lbm_lattice* L, int from, boo
     a.ntiles = L->ntiles;
     a.gtiles = L->gtiles;
     a.ngtiles = L->ngtiles;
+    a.links = L->use_links ? L->links : nullptr;
     if (moments) { a.mom_rho = L->mom[0]; a.mom_ux = L->mom[1]; a.mom_uy = L->mom[2]; }
     a.w = L->w; a.h = L->h; a.pitch = L->pitch; a.mpitch = L->mpitch; a.plane = L->plane;
     a.flags = L->flags;
@@ -457,6 +482,37 @@ __global__ void tile_flags_kernel(uint8_t* __restrict__ tflags, const uint8_t* _
         // wrapping path), 0 otherwise (the interior path wraps rows and its
         // edge columns at periodic edges itself).
         tflags[t] = gen ? ((solid_gen && !xedge && !yedge) ? 3 : 1) : ((xs + tile_w > w) ? 2 : 0);
+    }
+}
+
+__global__ void link_masks_kernel(uint4* __restrict__ links, const uint8_t* __restrict__ tflags,
+                                  const uint8_t* __restrict__ solid, int mpitch, int ntiles,
+                                  int h, int V, int frame, int halfway) {
+    const int64_t n = int64_t(h) * ntiles * 32;
+    for (int64_t q = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; q < n;
+         q += int64_t(gridDim.x) * blockDim.x) {
+        const int64_t t = q >> 5;
+        if (tflags[t] != 3) continue;
+        const int y = int(t / ntiles), tile = int(t - int64_t(y) * ntiles);
+        const int x0 = (tile * 32 + int(q & 31)) * V;
+        // a tile flagged 3 reaches no lattice edge: rows y - 1 .. y + 1 and
+        // columns x0 - 1 .. x0 + V are inside the lattice
+        uint32_t b[9] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
+        for (int k = 0; k < V; ++k) {
+            const int x = x0 + k;
+            b[0] |= uint32_t(solid[int64_t(y) * mpitch + x] != 0) << k;
+            if (!halfway) continue;
+            for (int i = 1; i < 9; ++i) {
+                const int sy = y - DROW(frame, i), sx = x - DCOL(frame, i);
+                b[i] |= uint32_t(solid[int64_t(sy) * mpitch + sx] != 0) << k;
+            }
+        }
+        uint4 o;
+        o.x = b[0] | (b[1] << 8) | (b[2] << 16) | (b[3] << 24);
+        o.y = b[4] | (b[5] << 8) | (b[6] << 16) | (b[7] << 24);
+        o.z = b[8];
+        o.w = 0u;
+        links[q] = o;
     }
 }
 
@@ -552,6 +608,7 @@ int lbm_destroy(lbm_lattice* L) {
         if (L->rb_landed) cudaEventDestroy(L->rb_landed);
         if (L->tflags) cudaFree(L->tflags);
         if (L->gtiles) cudaFree(L->gtiles);
+        if (L->links) cudaFree(L->links);
         if (L->own) cudaStreamDestroy(L->own);
     }
     delete L;

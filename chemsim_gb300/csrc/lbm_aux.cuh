@@ -129,6 +129,16 @@ __global__ void tile_flags_kernel(uint8_t* __restrict__ tflags, const uint8_t* _
                                   int w, int h, int mpitch, int tile_w, int ntiles, int xper,
                                   int yper);
 
+// Link masks of the tiles flagged 3 at V cells per thread: for lane l of tile
+// t (cells x0 = (tile * 32 + l) * V .. x0 + V - 1 of row y), byte 0 of
+// links[t * 32 + l] has bit k set when cell x0 + k is solid, and byte i
+// (i = 1..8), in half-way mode, when the source cell of direction i, (y,
+// x0 + k) minus the direction's displacement, is solid (that link bounces
+// back).  Tiles with another flag are not written.
+__global__ void link_masks_kernel(uint4* __restrict__ links, const uint8_t* __restrict__ tflags,
+                                  const uint8_t* __restrict__ solid, int mpitch, int ntiles,
+                                  int h, int V, int frame, int halfway);
+
 // Sets the message lbm_last_error_string returns on this thread.
 void set_last_error(const std::string& msg);
 

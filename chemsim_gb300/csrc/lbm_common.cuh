@@ -182,6 +182,27 @@ template <> struct Store<__nv_bfloat16> : DevStore<__nv_bfloat16, __nv_bfloat162
 constexpr float kHalfDevScale = 8192.0f;
 constexpr float kBf16DevScale = 1.0f;
 
+// Constants of the folded BGK collision of deviation variables on cell pairs
+// (collide_bgk_folded_x2), each value stored in both halves of a float2 so
+// that the packed f32x2 instructions read it as one 64-bit operand.  With
+// omega = dt/tau and the weight classes c = rest (w_0), axis (w_1 = w_2 = w_3
+// = w_4) and diagonal (w_5 = ... = w_8), omega G_eq_i + S_i (Guo) is
+//   [omega w_c D - sgw_c uF + a_c E_i + sgw_i cF4_i (c_i.u)] +- [a_c k1 (c_i.u) + sgw_i kcF_i]
+// (D = sum G, a_c = omega w_c s rho, E_i = k2 (c_i.u)^2 + k3 u^2, uF = k1 u.F):
+// the first bracket is even and the second odd under c_i -> -c_i, so a
+// direction pair (i, opp(i)) shares both, and out_i = keep G_i + that.
+struct PairConsts {
+    float2 keep;        // 1 - dt/tau
+    float2 ow[3];       // omega w_c
+    float2 owk[3];      // omega w_c k1
+    float2 k2, k3;
+    float2 k1fx, k1fy;  // k1 F: uF = ux k1fx + uy k1fy
+    float2 nsgw[3];     // -(s guo w_c)
+    float2 sgwcF4[9];   // s guo w_i cF4_i
+    float2 so[9];       // s guo w_i kcF_i
+    float2 dscale, shfx, shfy;
+};
+
 // Collision constants, computed on the host in the collision type exactly as
 // src/lbm.rs computes them (see lbm_api.cu: make_consts).
 template <class CT>
@@ -203,7 +224,36 @@ struct Consts {
     int collision;          // LBM_COLLISION_*
     int stochastic;         // 16-bit storage: stochastic rounding (not LBM_ROUND_NEAREST)
     int force;              // nonzero when a body force is set
+    PairConsts pk;          // the folded pair collision's constants (deviation storage)
 };
+
+// Fills c.pk from the scalar constants (host side, in double, rounded once).
+template <class CT>
+inline void fill_pair_consts(Consts<CT>& c) {
+    auto b = [](double v) { return make_float2(float(v), float(v)); };
+    const double om = -double(c.bgk_factor);
+    const double dev = double(c.dscale);
+    PairConsts& k = c.pk;
+    k.keep = b(1.0 + double(c.bgk_factor));
+    const int cls[3] = {0, 1, 5};
+    for (int q = 0; q < 3; ++q) {
+        const double wc = double(c.wt[cls[q]]);
+        k.ow[q] = b(om * wc);
+        k.owk[q] = b(om * wc * double(c.k1));
+        k.nsgw[q] = b(-dev * double(c.gw[cls[q]]));
+    }
+    k.k2 = b(double(c.k2));
+    k.k3 = b(double(c.k3));
+    k.k1fx = b(double(c.k1) * double(c.fx));
+    k.k1fy = b(double(c.k1) * double(c.fy));
+    for (int i = 0; i < 9; ++i) {
+        k.sgwcF4[i] = b(dev * double(c.gw[i]) * double(c.cF4[i]));
+        k.so[i] = b(dev * double(c.gw[i]) * double(c.kcF[i]));
+    }
+    k.dscale = b(dev);
+    k.shfx = b(double(c.shfx));
+    k.shfy = b(double(c.shfy));
+}
 
 // Arguments of one fused step over one lattice.
 template <class CT>
@@ -215,6 +265,8 @@ struct StepArgs {
     int ntiles;             // warp tiles per row (row stride of tflags)
     const uint32_t* gtiles; // listed tiles (row * ntiles + tile, bit 31: no lattice edge in reach), or null
     int ngtiles;
+    const uint4* links;     // 16-bit storage at 8 cells per thread: per (tile, lane) link masks of
+                            // the tiles flagged 3, which then take the interior path (or null)
     float* mom_rho;         // moment outputs (pitch `pitch`) or null
     float* mom_ux;
     float* mom_uy;

@@ -31,6 +31,9 @@ struct lbm_lattice {
     uint32_t* gtiles = nullptr;           // list of flagged tiles
     int ngtiles = 0;
     size_t gtiles_cap = 0;
+    uint4* links = nullptr;               // per (tile, lane) link masks (16-bit storage, 8 cells)
+    size_t links_cap = 0;                 // in uint4 entries
+    bool use_links = false;               // tiles flagged 3 run in the grid with the link masks
     int collision = LBM_COLLISION_BGK;
     float tau = 1.f, tau_minus = 1.f, dx = 1.f, dt = 1.f, fx = 0.f, fy = 0.f;
     float time = 0.f;

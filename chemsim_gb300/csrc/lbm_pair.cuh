@@ -89,8 +89,8 @@ __device__ __forceinline__ void collide_fast_x2(const Consts<float>& c, const fl
 }
 
 // Deviation variables G_i = s (f_i - w_i) (collide_dev on two cells).
-__device__ __forceinline__ void collide_dev_x2(const Consts<float>& c, const float2 (&G)[9],
-                                               float2 (&out)[9]) {
+__device__ __forceinline__ void collide_dev_x2_general(const Consts<float>& c,
+                                                       const float2 (&G)[9], float2 (&out)[9]) {
     const float2 DR = add2(add2(add2(add2(G[0], G[1]), add2(G[2], G[3])),
                                 add2(add2(G[4], G[5]), add2(G[6], G[7]))), G[8]);
     float2 jx = add2(add2(sub2(G[1], G[3]), sub2(G[5], G[6])), sub2(G[8], G[7]));
@@ -147,6 +147,75 @@ __device__ __forceinline__ void collide_dev_x2(const Consts<float>& c, const flo
         }
         out[0] = fma2(bc2(c.sgw[0]), sub2(bc2(c.kcF[0]), uF), out[0]);
     }
+}
+
+// BGK (with Guo forcing when a force is set) of deviation variables on two
+// cells, folded: out_i = G_i - omega (G_i - G_eq_i) + S_i is written as
+// keep G_i + (omega G_eq_i + S_i), and omega G_eq_i + S_i of a direction pair
+// (i, opp(i)) is even +- odd (PairConsts), so a pair costs one quadratic
+// term, two multiply-adds for the even part, one for the odd part and two
+// for the outputs.  The constants come as float2 pairs from the parameter
+// space.  Every term is of the size of the deviation, so the roundings stay
+// far below the 16-bit storage's own.  (Plain f32 populations keep the
+// general form: folded, keep f_i and omega f_eq_i are of the size of f_i,
+// and their roundings shift the mass step after step.)
+__device__ __forceinline__ void collide_bgk_folded_x2(const Consts<float>& c, const float2 (&G)[9],
+                                                      float2 (&out)[9]) {
+    const PairConsts& k = c.pk;
+    const float2 s13 = add2(G[1], G[3]), d13 = sub2(G[1], G[3]);
+    const float2 s24 = add2(G[2], G[4]), d24 = sub2(G[2], G[4]);
+    const float2 s57 = add2(G[5], G[7]), d57 = sub2(G[5], G[7]);
+    const float2 s68 = add2(G[6], G[8]), d68 = sub2(G[6], G[8]);
+    const float2 D = add2(add2(G[0], s13), add2(add2(s24, s57), s68));
+    float2 jx = sub2(add2(d13, d57), d68);            // c_x: 1, 5, 8 minus 3, 6, 7
+    float2 jy = add2(add2(d24, d57), d68);            // c_y: 2, 5, 6 minus 4, 7, 8
+    if (c.force) {
+        jx = add2(jx, k.shfx);
+        jy = add2(jy, k.shfy);
+    }
+    const float2 RS = add2(k.dscale, D);               // s rho
+    const float2 inv = rcp2(RS);
+    const float2 ux = mul2(jx, inv), uy = mul2(jy, inv);
+    const float2 ux2 = mul2(ux, ux), uy2 = mul2(uy, uy);
+    const float2 t3 = fma2(k.k3, ux2, mul2(k.k3, uy2));     // k3 u^2
+    const float2 d = add2(ux, uy), e = sub2(uy, ux);         // c.u of directions 5 and 6
+    float2 b0 = mul2(k.ow[0], D), b1 = mul2(k.ow[1], D), b5 = mul2(k.ow[2], D);
+    if (c.force) {
+        const float2 uF = fma2(ux, k.k1fx, mul2(uy, k.k1fy));
+        b0 = fma2(k.nsgw[0], uF, b0);
+        b1 = fma2(k.nsgw[1], uF, b1);
+        b5 = fma2(k.nsgw[2], uF, b5);
+    }
+    const float2 a0 = mul2(k.ow[0], RS), a1 = mul2(k.ow[1], RS), a5 = mul2(k.ow[2], RS);
+    const float2 a1k = mul2(k.owk[1], RS), a5k = mul2(k.owk[2], RS);
+    out[0] = fma2(G[0], k.keep, fma2(a0, t3, b0));
+    // one direction pair: cu = c_i.u, q = (c_i.u)^2, a / ak / b of its class
+    auto pair = [&](int i, int o, float2 cu, float2 q, float2 a, float2 ak, float2 b) {
+        float2 ee = fma2(a, fma2(k.k2, q, t3), b);
+        float2 oo;
+        if (c.force) {
+            ee = fma2(k.sgwcF4[i], cu, ee);
+            oo = fma2(ak, cu, k.so[i]);
+        } else {
+            oo = mul2(ak, cu);
+        }
+        out[i] = fma2(G[i], k.keep, add2(ee, oo));
+        out[o] = fma2(G[o], k.keep, sub2(ee, oo));
+    };
+    pair(1, 3, ux, ux2, a1, a1k, b1);
+    pair(2, 4, uy, uy2, a1, a1k, b1);
+    pair(5, 7, d, mul2(d, d), a5, a5k, b5);
+    pair(6, 8, e, mul2(e, e), a5, a5k, b5);
+}
+
+// The deviation collision on cell pairs: BGK folded, TRT general.
+#ifndef LBM_FOLDED_BGK
+#define LBM_FOLDED_BGK 1
+#endif
+__device__ __forceinline__ void collide_dev_x2(const Consts<float>& c, const float2 (&G)[9],
+                                               float2 (&out)[9]) {
+    if (LBM_FOLDED_BGK && c.collision != LBM_COLLISION_TRT) collide_bgk_folded_x2(c, G, out);
+    else collide_dev_x2_general(c, G, out);
 }
 
 }  // namespace lbmk

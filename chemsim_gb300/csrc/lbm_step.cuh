@@ -807,14 +807,23 @@ __device__ __forceinline__ uint32_t half_mask(uint32_t b, int j) {
     return (((b >> (2 * j)) & 1u) ? 0x0000ffffu : 0u) | (((b >> (2 * j + 1)) & 1u) ? 0xffff0000u : 0u);
 }
 
-// Interior warp tile (flag 0) of 16-bit storage, packed.
+// Interior warp tile (flag 0) of 16-bit storage, packed.  With `gen` (a tile
+// flagged 3 of a lattice with link masks: solids nearby, no lattice edge in
+// reach) the same code runs with the fixups of step_general_packed, read from
+// the tile's precomputed per-lane link masks instead of the mask rows:
+// bounce-back links take the cell's own opposite population, and solid cells
+// are swapped (full-way) or keep their populations (half-way).  Both kinds of
+// tile then share one copy of the collision code.
 template <class S, int V, int FRAME, bool SR>
 __device__ __forceinline__ void step_interior_packed(const StepArgs<float>& a, int y, int x0,
-                                                     int lane) {
+                                                     int lane, int tile = 0, bool gen = false) {
     constexpr int NP = V / 2;
+    constexpr uint32_t FULL = (1u << V) - 1u;
     const unsigned short* __restrict__ src = static_cast<const unsigned short*>(a.src);
     const int64_t PL = a.plane;
     const InteriorRows rows(a, y, x0, V);
+    uint4 lk = make_uint4(0u, 0u, 0u, 0u);
+    if (V == 8 && gen) lk = __ldg(a.links + (int64_t(y) * a.ntiles + tile) * 32 + lane);
     uint32_t r[9][NP];
     uint32_t edge[9];
 #pragma unroll
@@ -838,7 +847,55 @@ __device__ __forceinline__ void step_interior_packed(const StepArgs<float>& a, i
             shift_down_packed<NP>(r[i], lane == 31 ? edge[i] : right);
         }
     }
-    collide_store_packed<S, V, SR, (V / 2 >= 4) && LBM_ROLL_INTERIOR>(a, y, x0, r);
+    uint32_t own_solid = 0u;
+    const bool halfway = (a.flags & LBM_SOLID_HALFWAY) != 0;
+    if (V == 8 && gen) {
+        own_solid = lk.x & FULL;
+        const uint32_t words[3] = {lk.x, lk.y, lk.z};
+        // bounce-back links take the cell's own opposite population
+#pragma unroll
+        for (int i = 1; i < 9; ++i) {
+            const uint32_t bnc = (words[i >> 2] >> (8 * (i & 3))) & FULL;
+            if (bnc) {
+                uint32_t ld[NP];
+                PackIO<NP>::load(src + OPP(i) * PL + rows.r0 + x0, ld);
+#pragma unroll
+                for (int j = 0; j < NP; ++j) {
+                    const uint32_t m = half_mask(bnc, j);
+                    r[i][j] = (r[i][j] & ~m) | (ld[j] & m);
+                }
+            }
+        }
+        if (own_solid && !halfway) {
+            // bounce_back (src/lbm.rs:741-751): solid nodes take swapped populations
+#pragma unroll
+            for (int p = 0; p < 4; ++p) {
+                const int i0 = p < 2 ? 1 + p : 5 + (p - 2), i1 = OPP(i0);
+#pragma unroll
+                for (int j = 0; j < NP; ++j) {
+                    const uint32_t m = half_mask(own_solid, j);
+                    const uint32_t t = (r[i0][j] ^ r[i1][j]) & m;
+                    r[i0][j] ^= t;
+                    r[i1][j] ^= t;
+                }
+            }
+        }
+    }
+    collide_packed<S, V, SR, false, (V / 2 >= 4) && LBM_ROLL_INTERIOR>(a.c, r);
+    if (V == 8 && gen && own_solid && halfway) {
+        // half-way mode: solid nodes keep their populations
+#pragma unroll
+        for (int i = 0; i < 9; ++i) {
+            uint32_t ld[NP];
+            PackIO<NP>::load(src + i * PL + rows.r0 + x0, ld);
+#pragma unroll
+            for (int j = 0; j < NP; ++j) {
+                const uint32_t m = half_mask(own_solid, j);
+                r[i][j] = (r[i][j] & ~m) | (ld[j] & m);
+            }
+        }
+    }
+    store_packed<S, V>(a, y, x0, r);
 }
 
 // Periodic-edge warp tile (flag 2) of 16-bit storage, packed (the rules of
@@ -1326,12 +1383,14 @@ lbm_step_kernel(const StepArgs<typename Store<S>::CT> a) {
         return;
     }
     const uint8_t flag = a.tflags[int64_t(y) * a.ntiles + tile];        // warp-uniform
-    if (flag & 1) return;                                                  // 1, 3: owned by the list
     const int x0 = (tile * 32 + threadIdx.x) * V;
     if constexpr (Store<S>::DEV && LBM_PACKED16) {
-        if (flag == 0) step_interior_packed<S, V, FRAME, SR>(a, y, x0, threadIdx.x);
-        else step_interior_wrap_packed<S, V, FRAME, SR>(a, y, x0, threadIdx.x);
+        // 1 and 3 are owned by the list, except 3 when link masks exist
+        if (flag == 1 || (flag == 3 && a.links == nullptr)) return;
+        if (flag == 2) step_interior_wrap_packed<S, V, FRAME, SR>(a, y, x0, threadIdx.x);
+        else step_interior_packed<S, V, FRAME, SR>(a, y, x0, threadIdx.x, tile, flag == 3);
     } else {
+        if (flag & 1) return;                                              // 1, 3: owned by the list
         if (flag == 0) step_interior<S, V, FRAME, FAST, SR>(a, y, x0, threadIdx.x);
         else step_interior_wrap<S, V, FRAME, FAST, SR>(a, y, x0, threadIdx.x);
     }
