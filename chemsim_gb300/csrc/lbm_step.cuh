@@ -807,16 +807,29 @@ __device__ __forceinline__ uint32_t half_mask(uint32_t b, int j) {
     return (((b >> (2 * j)) & 1u) ? 0x0000ffffu : 0u) | (((b >> (2 * j + 1)) & 1u) ? 0xffff0000u : 0u);
 }
 
-// Interior warp tile (flag 0) of 16-bit storage, packed.  With `gen` (a tile
+// Tiles flagged 3 run a second instantiation of the interior code (GEN):
+// with LBM_GEN_OWN it loads the cells' own populations up front, with
+// LBM_ROLL_GEN its pair loop is rolled (fewer registers: the unrolled form
+// spilled).  A/B on one GB300, 4096^2 channel, 16-bit stochastic: fixups as a
+// run-time branch of the interior code 149.0k MLUPS (the branch also slowed
+// the pure interior path 4%); separate instantiation 151.4k; + own loads
+// 152.4k; + rolled 153.8k; both 154.8k.
+#ifndef LBM_GEN_OWN
+#define LBM_GEN_OWN 1
+#endif
+#ifndef LBM_ROLL_GEN
+#define LBM_ROLL_GEN 1
+#endif
+// Interior warp tile (flag 0) of 16-bit storage, packed.  With GEN_CT (a tile
 // flagged 3 of a lattice with link masks: solids nearby, no lattice edge in
 // reach) the same code runs with the fixups of step_general_packed, read from
 // the tile's precomputed per-lane link masks instead of the mask rows:
 // bounce-back links take the cell's own opposite population, and solid cells
-// are swapped (full-way) or keep their populations (half-way).  Both kinds of
-// tile then share one copy of the collision code.
-template <class S, int V, int FRAME, bool SR>
+// are swapped (full-way) or keep their populations (half-way).
+template <class S, int V, int FRAME, bool SR, bool GEN_CT = false>
 __device__ __forceinline__ void step_interior_packed(const StepArgs<float>& a, int y, int x0,
-                                                     int lane, int tile = 0, bool gen = false) {
+                                                     int lane, int tile = 0) {
+    constexpr bool gen = GEN_CT;
     constexpr int NP = V / 2;
     constexpr uint32_t FULL = (1u << V) - 1u;
     const unsigned short* __restrict__ src = static_cast<const unsigned short*>(a.src);
@@ -834,6 +847,21 @@ __device__ __forceinline__ void step_interior_packed(const StepArgs<float>& a, i
         edge[i] = 0u;
         if (dc == 1 && lane == 0) edge[i] = uint32_t(__ldg(prow + rows.left)) << 16;
         if (dc == -1 && lane == 31) edge[i] = __ldg(prow + rows.right);
+    }
+    // LBM_GEN_OWN: tiles flagged 3 load the cell's own populations (row y of
+    // every plane) with everything else, so the bounce-back links and the
+    // half-way keep need no second and third memory round trip; planes
+    // without a row shift take them from their load before the column shift.
+    uint32_t own[9][NP];
+    if constexpr (LBM_GEN_OWN && GEN_CT && V == 8) {
+#pragma unroll
+        for (int i = 0; i < 9; ++i) {
+            if (DROW(FRAME, i) != 0) PackIO<NP>::load(src + i * PL + rows.r0 + x0, own[i]);
+            else {
+#pragma unroll
+                for (int j = 0; j < NP; ++j) own[i][j] = r[i][j];
+            }
+        }
     }
     prefetch_ahead<S, V, FRAME>(a, y, x0, lane);
 #pragma unroll
@@ -858,7 +886,12 @@ __device__ __forceinline__ void step_interior_packed(const StepArgs<float>& a, i
             const uint32_t bnc = (words[i >> 2] >> (8 * (i & 3))) & FULL;
             if (bnc) {
                 uint32_t ld[NP];
-                PackIO<NP>::load(src + OPP(i) * PL + rows.r0 + x0, ld);
+                if constexpr (LBM_GEN_OWN && GEN_CT) {
+#pragma unroll
+                    for (int j = 0; j < NP; ++j) ld[j] = own[OPP(i)][j];
+                } else {
+                    PackIO<NP>::load(src + OPP(i) * PL + rows.r0 + x0, ld);
+                }
 #pragma unroll
                 for (int j = 0; j < NP; ++j) {
                     const uint32_t m = half_mask(bnc, j);
@@ -881,13 +914,19 @@ __device__ __forceinline__ void step_interior_packed(const StepArgs<float>& a, i
             }
         }
     }
-    collide_packed<S, V, SR, false, (V / 2 >= 4) && LBM_ROLL_INTERIOR>(a.c, r);
+    collide_packed<S, V, SR, false,
+                   (V / 2 >= 4) && (GEN_CT ? LBM_ROLL_GEN : LBM_ROLL_INTERIOR)>(a.c, r);
     if (V == 8 && gen && own_solid && halfway) {
         // half-way mode: solid nodes keep their populations
 #pragma unroll
         for (int i = 0; i < 9; ++i) {
             uint32_t ld[NP];
-            PackIO<NP>::load(src + i * PL + rows.r0 + x0, ld);
+            if constexpr (LBM_GEN_OWN && GEN_CT) {
+#pragma unroll
+                for (int j = 0; j < NP; ++j) ld[j] = own[i][j];
+            } else {
+                PackIO<NP>::load(src + i * PL + rows.r0 + x0, ld);
+            }
 #pragma unroll
             for (int j = 0; j < NP; ++j) {
                 const uint32_t m = half_mask(own_solid, j);
@@ -1388,7 +1427,8 @@ lbm_step_kernel(const StepArgs<typename Store<S>::CT> a) {
         // 1 and 3 are owned by the list, except 3 when link masks exist
         if (flag == 1 || (flag == 3 && a.links == nullptr)) return;
         if (flag == 2) step_interior_wrap_packed<S, V, FRAME, SR>(a, y, x0, threadIdx.x);
-        else step_interior_packed<S, V, FRAME, SR>(a, y, x0, threadIdx.x, tile, flag == 3);
+        else if (flag == 3) step_interior_packed<S, V, FRAME, SR, true>(a, y, x0, threadIdx.x, tile);
+        else step_interior_packed<S, V, FRAME, SR>(a, y, x0, threadIdx.x);
     } else {
         if (flag & 1) return;                                              // 1, 3: owned by the list
         if (flag == 0) step_interior<S, V, FRAME, FAST, SR>(a, y, x0, threadIdx.x);
