@@ -38,6 +38,7 @@ struct lbm_batch {
     bool built = false;
     int frame = 0, fast = 1;
     int grid[6] = {0, 0, 0, 0, 0, 0};  // per list: resident blocks of its kernel x SMs
+    int grid_fused = 0;               // the same for the fused kernel
     cudaStream_t own = nullptr, stream = nullptr;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     int dev = 0;
@@ -57,6 +58,15 @@ constexpr int kBatchGraphSteps = 16;
 #endif
 #ifndef LBM_BATCH_PREFETCH
 #define LBM_BATCH_PREFETCH 1
+#endif
+// 1: every step is one launch of the fused kernel over all items; 0 (the
+// default): one launch per non-empty list, each of its own kernel.  A/B on
+// one GB300 (512 members, 154 M cells, autotuned): fused 0.566 of the copy
+// bandwidth, lists 0.680.  The fused kernel takes the registers of its
+// largest path (the general step, 128 a thread), so the lean items, which
+// need 80, run at two thirds of their occupancy.
+#ifndef LBM_BATCH_FUSED
+#define LBM_BATCH_FUSED 0
 #endif
 
 // One warp = one work item; a warp walks its item list with a stride of the
@@ -82,7 +92,7 @@ lbm_batch_kernel(const lbm_batch_member_dev* __restrict__ members, const uint2* 
             // L2 prefetch of the rows the next item pulls, one plane a lane
             // (the range is clipped to the row's pitch, so it stays inside
             // the member's buffer)
-            const StepArgs<float>& an = members[next.x].a[parity];
+            const StepArgs<float>& an = members[next.x & 0xffffffu].a[parity];
             const int ys = int(next.y >> 12) - DROW(FRAME, lane);
             const int x0 = int(next.y & 4095u) * 32 * V;
             if (ys >= 0 && ys < an.h) {
@@ -92,7 +102,7 @@ lbm_batch_kernel(const lbm_batch_member_dev* __restrict__ members, const uint2* 
                 asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" :: "l"(p), "r"(n * 4) : "memory");
             }
         }
-        const StepArgs<float>& a = members[item.x].a[parity];
+        const StepArgs<float>& a = members[item.x & 0xffffffu].a[parity];
         const int y = int(item.y >> 12), tile = int(item.y & 4095u);
         if constexpr (PATH == 1) step_general<float, V, FRAME, FAST>(a, y, tile, lane);
         else if constexpr (PATH == 2) step_interior_wrap<float, V, FRAME, FAST>(a, y, (tile * 32 + lane) * V, lane);
@@ -101,7 +111,53 @@ lbm_batch_kernel(const lbm_batch_member_dev* __restrict__ members, const uint2* 
     }
 }
 
+// All item kinds in one persistent kernel: item word x carries the member
+// index in its low 24 bits and the list (tile width and path) in bits 24-26,
+// and the warp dispatches on it, so a step is one launch.  Lists stay in
+// order (general items first, so their longer latency overlaps the rest).
+template <int FRAME, bool FAST>
+__global__ void __launch_bounds__(256, 2)
+lbm_batch_fused_kernel(const lbm_batch_member_dev* __restrict__ members,
+                       const uint2* __restrict__ items, int nitems, int parity) {
+    const int lane = threadIdx.x;
+    const int warps = gridDim.x * blockDim.y;
+    int it = blockIdx.x * blockDim.y + threadIdx.y;
+    uint2 item = it < nitems ? items[it] : make_uint2(0u, 0u);
+    for (; it < nitems; it += warps) {
+        const uint2 next = it + warps < nitems ? items[it + warps] : make_uint2(0u, 0u);
+        const int m = int(item.x & 0xffffffu), k = int(item.x >> 24);
+        if (LBM_BATCH_PREFETCH && lane < 9 && it + warps < nitems) {
+            const int nk = int(next.x >> 24), nv = nk < 3 ? 2 : 4;
+            const StepArgs<float>& an = members[next.x & 0xffffffu].a[parity];
+            const int ys = int(next.y >> 12) - DROW(FRAME, lane);
+            const int x0 = int(next.y & 4095u) * 32 * nv;
+            if (ys >= 0 && ys < an.h) {
+                const int n = min(32 * nv, an.pitch - x0);
+                const float* p = static_cast<const float*>(an.src) + lane * an.plane +
+                                 int64_t(ys) * an.pitch + x0;
+                asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" :: "l"(p), "r"(n * 4) : "memory");
+            }
+        }
+        const StepArgs<float>& a = members[m].a[parity];
+        const int y = int(item.y >> 12), tile = int(item.y & 4095u);
+        switch (k) {     // warp-uniform
+            case 0: step_general<float, 2, FRAME, FAST>(a, y, tile, lane); break;
+            case 1: step_interior_wrap<float, 2, FRAME, FAST>(a, y, (tile * 32 + lane) * 2, lane); break;
+            case 2: step_interior<float, 2, FRAME, FAST>(a, y, (tile * 32 + lane) * 2, lane); break;
+            case 3: step_general<float, 4, FRAME, FAST>(a, y, tile, lane); break;
+            case 4: step_interior_wrap<float, 4, FRAME, FAST>(a, y, (tile * 32 + lane) * 4, lane); break;
+            default: step_interior<float, 4, FRAME, FAST>(a, y, (tile * 32 + lane) * 4, lane); break;
+        }
+        item = next;
+    }
+}
+
 using BatchKernel = void (*)(const lbm_batch_member_dev*, const uint2*, int, int);
+
+BatchKernel pick_fused(int frame, int fast) {
+    if (frame) return fast ? lbm_batch_fused_kernel<1, true> : lbm_batch_fused_kernel<1, false>;
+    return fast ? lbm_batch_fused_kernel<0, true> : lbm_batch_fused_kernel<0, false>;
+}
 
 template <int V, int PATH>
 BatchKernel pick_kernel_v(int frame, int fast) {
@@ -171,7 +227,8 @@ int ensure_table(lbm_batch* B) {
             for (int t = 0; t < L->ntiles; ++t) {
                 const uint8_t fl = flags[size_t(r) * L->ntiles + t];
                 const int j = (fl & 1) ? 0 : (fl == 2 ? 1 : 2);     // 1, 3: general
-                lists[vbase + j].push_back(make_uint2(uint32_t(i), (uint32_t(r) << 12) | uint32_t(t)));
+                lists[vbase + j].push_back(make_uint2(uint32_t(i) | (uint32_t(vbase + j) << 24),
+                                                      (uint32_t(r) << 12) | uint32_t(t)));
             }
     }
     std::vector<uint2> tasks;
@@ -203,6 +260,13 @@ int ensure_table(lbm_batch* B) {
 // One step: for each tile width, the general items, then the periodic-edge
 // and the lean interior items, one launch per non-empty list.
 cudaError_t launch(lbm_batch* B, int parity) {
+    if (LBM_BATCH_FUSED) {
+        if (B->ntasks == 0) return cudaSuccess;
+        const int grid = std::min(B->grid_fused, (B->ntasks + kTaskWarps - 1) / kTaskWarps);
+        pick_fused(B->frame, B->fast)<<<grid, dim3(32, kTaskWarps), 0, B->stream>>>(
+            B->d_members, B->d_tasks, B->ntasks, parity);
+        return cudaGetLastError();
+    }
     for (int k = 0; k < kLists; ++k) {
         const int n = B->list_off[k + 1] - B->list_off[k];
         if (n == 0) continue;
@@ -302,6 +366,12 @@ int lbm_batch_create(int n, const lbm_desc* descs, int flags, lbm_batch** out) {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pick_kernel(k, B->frame, B->fast),
                                                       32 * kTaskWarps, 0);
         B->grid[k] = std::max(1, sms) * std::max(1, per_sm);
+    }
+    {
+        int per_sm = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pick_fused(B->frame, B->fast),
+                                                      32 * kTaskWarps, 0);
+        B->grid_fused = std::max(1, sms) * std::max(1, per_sm);
     }
     *out = B;
     return LBM_OK;
@@ -427,6 +497,7 @@ int lbm_batch_autotune(lbm_batch* B, const char* cache_path, int steps_per_trial
         view.frame = B->frame;
         view.fast = B->fast;
         std::copy(B->grid, B->grid + kLists, view.grid);
+        view.grid_fused = B->grid_fused;
         view.stream = B->stream;
         view.dev = B->dev;
         struct Saved { void* f; int cur; float time; int64_t steps; int v, rows; };
