@@ -13,13 +13,15 @@ populations per step) are larger than L2, so no L2 flush is needed.
           lattice's stream, max over ranks.
   e2e     the same metric through the C ABI with host buffers: the initial
           fields are uploaded from pinned host memory and, every frame of two
-          steps (the reference demo's speed_factor, src/main.rs:393), rho/u are
-          read back into pinned host memory (LBMSim::step + render,
-          src/main.rs:128-177) with lbm_read_moments_async, whose host copy
-          overlaps the next frame's steps; the last copy is waited for inside
-          the timed region.  e2e.blocking_readback: the same loop with the
-          blocking lbm_read_moments; e2e.rendered_frames: reading back the
-          finished RGBA8 frame of lbm_render_async (render.rs's colour map).
+          steps (the reference demo's speed_factor, src/main.rs:393), rho/u
+          reach pinned host memory (LBMSim::step + render, src/main.rs:128-177):
+          written by the frame's last step kernel straight into the host
+          buffers (lbm_step_moments_to); the last frame is waited for inside
+          the timed region.  e2e.async_copy_readback: staged on the device and
+          copied with lbm_read_moments_async, the copy overlapping the next
+          frame's steps; e2e.blocking_readback: the blocking lbm_read_moments;
+          e2e.rendered_frames: reading back the finished RGBA8 frame of
+          lbm_render_async (render.rs's colour map).
   fp16    the same lattice with half-precision deviation storage: the default
           stochastic rounding, and round_nearest (LBM_ROUND_NEAREST).
   accuracy  rho/u L2 errors of f32/f16/bf16 storage against the f64 run of
@@ -365,7 +367,8 @@ def run_ours(args):
     lat16n.close()
 
     # e2e through the C ABI with pinned host buffers
-    e2e = run_e2e(spec, args, torch, dist)
+    e2e = run_e2e(spec, args, torch, dist, readback="mapped")
+    e2e["async_copy_readback"] = run_e2e(spec, args, torch, dist)
     e2e["blocking_readback"] = run_e2e(spec, args, torch, dist, readback="moments")
     e2e["rendered_frames"] = run_e2e(spec, args, torch, dist, readback="frame")
     batch = None if args.no_batch or world > 1 else run_batch(args, torch)
@@ -650,14 +653,20 @@ def run_e2e(spec, args, torch, dist, readback="async"):
       "moments" the same fields with the blocking lbm_read_moments;
       "frame"   the finished RGBA8 velocity frame of lbm_render_async (the
                 colour map of render.rs on the device) into two alternating
-                pinned images, overlapped like "async"."""
+                pinned images, overlapped like "async";
+      "mapped"  rho/u written by each frame's last step kernel straight into
+                two alternating pinned host buffer sets (lbm_step_moments_to),
+                no staging copy; the last frame is waited for inside the timed
+                region."""
     from chemsim_gb300 import lbm
     from chemsim_gb300._lib import check
     flags = spec.flags | (0 if args.strict else lbm.FAST)
     pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()  # noqa: E731
     rho, ux, uy = pin(spec.rho), pin(spec.ux), pin(spec.uy)
-    outs = [[torch.empty((spec.h, spec.w), dtype=torch.float32).pin_memory().numpy()
-             for _ in range(3)] for _ in range(2)]
+    pinned = [[torch.empty((spec.h, spec.w), dtype=torch.float32).pin_memory() for _ in range(3)]
+              for _ in range(2)]
+    outs = [[t.numpy() for t in group] for group in pinned]
+    ptrs = [[t.data_ptr() for t in group] for group in pinned]
     imgs = [torch.empty((spec.h, spec.w, 4), dtype=torch.uint8).pin_memory().numpy()
             for _ in range(2)]
     lat = lbm.Lattice(spec.w, spec.h, spec.tau, lbm.F32, flags)
@@ -676,6 +685,9 @@ def run_e2e(spec, args, torch, dist, readback="async"):
     t0 = time.perf_counter()
     lat.init_equilibrium(rho, ux, uy)
     for k in range(frames):
+        if readback == "mapped":
+            lat.step_moments_to(2, *ptrs[k & 1])
+            continue
         lat.step_moments(2)
         if readback == "async":
             lat.read_moments_async(*outs[k & 1])
@@ -697,7 +709,10 @@ def run_e2e(spec, args, torch, dist, readback="async"):
     cells = spec.w * spec.h
     steps = 2 * frames
     per_frame = 4 * cells if readback == "frame" else 3 * 4 * cells
-    notes = {"async": "rho/ux/uy every frame, lbm_read_moments_async into alternating pinned "
+    notes = {"mapped": "rho/ux/uy every frame, written by the frame's last step kernel straight "
+                       "into alternating pinned host buffers (lbm_step_moments_to, over the "
+                       "host link; no staging copy)",
+             "async": "rho/ux/uy every frame, lbm_read_moments_async into alternating pinned "
                       "buffers (copy overlaps the next frame's steps)",
              "moments": "rho/ux/uy every frame, blocking lbm_read_moments",
              "frame": "one RGBA8 velocity frame every frame (lbm_render_async, render.rs colour "

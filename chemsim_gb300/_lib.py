@@ -115,6 +115,7 @@ SIGNATURES = {
     "lbm_batch_set_stream": (_i32, [_vp, _vp]),
     "lbm_batch_autotune": (_i32, [_vp, ctypes.c_char_p, _i32]),
     "lbm_read_moments_async": (_i32, [_vp, _vp, _vp, _vp]),
+    "lbm_step_moments_to": (_i32, [_vp, _i32, _vp, _vp, _vp]),
     "lbm_readback_wait": (_i32, [_vp]),
     "lbm_render": (_i32, [_vp, _i32, _i32, _vp, _i32]),
     "lbm_render_async": (_i32, [_vp, _i32, _i32, _vp]),

@@ -141,6 +141,27 @@ cudaError_t launch_one_t(lbm_lattice* L, int from, bool moments) {
                           (L->flags & LBM_FAST) != 0, L->vcells, L->rows, L->stream);
 }
 
+// One step whose moments go to out[0..2] (dense rows of w elements).
+template <class S>
+cudaError_t launch_to_t(lbm_lattice* L, float* const* out) {
+    StepArgs<typename Store<S>::CT> a = lattice_args<S>(L, L->cur, false);
+    a.mom_rho = out[0];
+    a.mom_ux = out[1];
+    a.mom_uy = out[2];
+    a.mom_pitch = L->w;
+    return launch_step<S>(a, (L->flags & LBM_FRAME_XY) ? 1 : 0, (L->flags & LBM_FAST) != 0,
+                          L->vcells, L->rows, L->stream);
+}
+
+cudaError_t launch_one_to(lbm_lattice* L, float* const* out) {
+    switch (L->precision) {
+        case LBM_F32: return launch_to_t<float>(L, out);
+        case LBM_F64: return launch_to_t<double>(L, out);
+        case LBM_F16DEV: return launch_to_t<__half>(L, out);
+        default: return launch_to_t<__nv_bfloat16>(L, out);
+    }
+}
+
 cudaError_t launch_one(lbm_lattice* L, int from, bool moments) {
     switch (L->precision) {
         case LBM_F32: return launch_one_t<float>(L, from, moments);
@@ -157,11 +178,12 @@ void drop_graphs(lbm_lattice* L) {
     }
 }
 
-int ensure_graph(lbm_lattice* L) {
+// Captures the kGraphSteps-step graph that starts from buffer `start`.
+int ensure_graph(lbm_lattice* L, int start) {
     if (L->dirty) { drop_graphs(L); L->dirty = false; }
-    if (L->graph[L->cur]) return LBM_OK;
+    if (L->graph[start]) return LBM_OK;
     LBM_CUDA(cudaStreamBeginCapture(L->stream, cudaStreamCaptureModeThreadLocal));
-    int from = L->cur;
+    int from = start;
     cudaError_t err = cudaSuccess;
     for (int s = 0; s < kGraphSteps && err == cudaSuccess; ++s) {
         err = launch_one(L, from, false);
@@ -171,9 +193,9 @@ int ensure_graph(lbm_lattice* L) {
     cudaError_t e2 = cudaStreamEndCapture(L->stream, &g);
     if (err != cudaSuccess) { if (g) cudaGraphDestroy(g); return cuda_fail(err, "step capture"); }
     if (e2 != cudaSuccess) return cuda_fail(e2, "cudaStreamEndCapture");
-    cudaError_t e3 = cudaGraphInstantiate(&L->graph[L->cur], g, 0);
+    cudaError_t e3 = cudaGraphInstantiate(&L->graph[start], g, 0);
     cudaGraphDestroy(g);
-    if (e3 != cudaSuccess) { L->graph[L->cur] = nullptr; return cuda_fail(e3, "cudaGraphInstantiate"); }
+    if (e3 != cudaSuccess) { L->graph[start] = nullptr; return cuda_fail(e3, "cudaGraphInstantiate"); }
     return LBM_OK;
 }
 
@@ -368,10 +390,26 @@ int steps_impl(lbm_lattice* L, int nsteps, bool moments) {
     const int plain = moments ? nsteps - 1 : nsteps;
     const int full = plain / kGraphSteps;
     const int rem = plain % kGraphSteps;
-    if (full > 0) {
-        int rc = ensure_graph(L);
-        if (rc) return rc;
-        for (int k = 0; k < full; ++k) LBM_CUDA(cudaGraphLaunch(L->graph[L->cur], L->stream));
+    // The graphs of both buffer parities are captured at the first step call
+    // after any change of the step arguments, so a long run that follows a
+    // few short ones does not pay for the capture.
+    // While the caller captures the stream into a graph of its own, the
+    // steps are plain launches (captured there).
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    LBM_CUDA(cudaStreamIsCapturing(L->stream, &cap));
+    const bool capturing = cap != cudaStreamCaptureStatusNone;
+    if (!capturing)
+        for (int p = 0; p < 2; ++p)
+            if (int rc = ensure_graph(L, p)) return rc;
+    for (int k = 0; k < full; ++k) {
+        if (capturing) {
+            for (int s = 0; s < kGraphSteps; ++s) {
+                LBM_CUDA(launch_one(L, L->cur, false));
+                L->cur ^= 1;
+            }
+        } else {
+            LBM_CUDA(cudaGraphLaunch(L->graph[L->cur], L->stream));
+        }
     }
     for (int k = 0; k < rem; ++k) {
         LBM_CUDA(launch_one(L, L->cur, false));
@@ -408,6 +446,7 @@ StepArgs<typename Store<S>::CT> lattice_args(const lbm_lattice* L, int from, boo
     a.ngtiles = L->ngtiles;
     a.links = L->use_links ? L->links : nullptr;
     if (moments) { a.mom_rho = L->mom[0]; a.mom_ux = L->mom[1]; a.mom_uy = L->mom[2]; }
+    a.mom_pitch = L->pitch;
     a.w = L->w; a.h = L->h; a.pitch = L->pitch; a.mpitch = L->mpitch; a.plane = L->plane;
     a.flags = L->flags;
     a.pf_rows = -1;          // the launcher sizes the L2 prefetch distance
@@ -793,6 +832,41 @@ int lbm_read_moments_async(lbm_lattice* L, float* rho, float* ux, float* uy) {
         LBM_CUDA(cudaMemcpyAsync(dst[m], L->rb + m * plane, plane * sizeof(float),
                                  cudaMemcpyDeviceToHost, L->rb_stream));
     LBM_CUDA(cudaEventRecord(L->rb_landed, L->rb_stream));
+    L->rb_pending = true;
+    return LBM_OK;
+}
+
+int lbm_step_moments_to(lbm_lattice* L, int nsteps, float* rho, float* ux, float* uy) {
+    if (int rc = check_handle(L)) return rc;
+    if (nsteps < 1) return fail(LBM_ERR_INVALID_ARGUMENT, "lbm_step_moments_to needs nsteps >= 1");
+    if (!rho || !ux || !uy) return fail(LBM_ERR_INVALID_ARGUMENT, "null field pointer");
+    DeviceGuard g(L->dev);
+    // Only memory the GPU can address is accepted: device or managed
+    // allocations, and pinned host memory (its device alias is used).
+    float* out[3] = {rho, ux, uy};
+    for (int m = 0; m < 3; ++m) {
+        cudaPointerAttributes at{};
+        cudaError_t e = cudaPointerGetAttributes(&at, out[m]);
+        if (e != cudaSuccess || at.type == cudaMemoryTypeUnregistered || at.devicePointer == nullptr) {
+            (void)cudaGetLastError();
+            return fail(LBM_ERR_INVALID_ARGUMENT,
+                        "lbm_step_moments_to writes device memory or pinned host memory "
+                        "(cudaHostAlloc / cudaHostRegister); this pointer is neither");
+        }
+        out[m] = static_cast<float*>(at.devicePointer);
+    }
+    // the previous readback into these (or other) buffers must have landed
+    // before the host reads: lbm_readback_wait covers both kinds
+    if (L->rb_pending) LBM_CUDA(cudaStreamWaitEvent(L->stream, L->rb_landed, 0));
+    if (nsteps > 1)
+        if (int rc = steps_impl(L, nsteps - 1, false)) return rc;
+    if (int rc = lattice_readback_stream(L)) return rc;
+    LBM_CUDA(launch_one_to(L, out));
+    L->cur ^= 1;
+    L->time += L->dt;
+    L->steps += 1;
+    L->mom_valid = false;
+    LBM_CUDA(cudaEventRecord(L->rb_landed, L->stream));
     L->rb_pending = true;
     return LBM_OK;
 }

@@ -270,6 +270,7 @@ struct StepArgs {
     float* mom_rho;         // moment outputs (pitch `pitch`) or null
     float* mom_ux;
     float* mom_uy;
+    int mom_pitch;          // row stride of the moment outputs in elements
     int w, h, pitch, mpitch;
     int64_t plane;          // plane stride in elements
     int flags;

@@ -450,17 +450,41 @@ __device__ __forceinline__ void store_cells(const StepArgs<typename Store<S>::CT
                 if (x0 + k < w) dst[i * PL + base + k] = enc[i][k];
     }
     if (a.mom_rho != nullptr) {
+        const int64_t mbase = int64_t(y) * a.mom_pitch + x0;
+        float mr[V], mx[V], my[V];
 #pragma unroll
         for (int k = 0; k < V; ++k) {
-            if (x0 + k >= w) break;
             CT g[9];
 #pragma unroll
             for (int i = 0; i < 9; ++i) g[i] = ST::dec_dom(enc[i][k]);
             CT r, ux, uy;
             domain_moments<S, FAST>(a.c, g, r, ux, uy);
-            a.mom_rho[base + k] = float(r);
-            a.mom_ux[base + k] = float(ux);
-            a.mom_uy[base + k] = float(uy);
+            mr[k] = float(r);
+            mx[k] = float(ux);
+            my[k] = float(uy);
+        }
+        // whole, 16-byte aligned runs go out as vectors (the outputs may be
+        // host memory written over the host link, where wide writes matter)
+        if constexpr (V % 4 == 0) {
+            const bool aligned = ((reinterpret_cast<uintptr_t>(a.mom_rho) |
+                                   reinterpret_cast<uintptr_t>(a.mom_ux) |
+                                   reinterpret_cast<uintptr_t>(a.mom_uy)) & 15u) == 0;
+            if (aligned && x0 + V <= w && (mbase & 3) == 0) {
+#pragma unroll
+                for (int k = 0; k < V; k += 4) {
+                    *reinterpret_cast<float4*>(a.mom_rho + mbase + k) = make_float4(mr[k], mr[k + 1], mr[k + 2], mr[k + 3]);
+                    *reinterpret_cast<float4*>(a.mom_ux + mbase + k) = make_float4(mx[k], mx[k + 1], mx[k + 2], mx[k + 3]);
+                    *reinterpret_cast<float4*>(a.mom_uy + mbase + k) = make_float4(my[k], my[k + 1], my[k + 2], my[k + 3]);
+                }
+                return;
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < V; ++k) {
+            if (x0 + k >= w) break;
+            a.mom_rho[mbase + k] = mr[k];
+            a.mom_ux[mbase + k] = mx[k];
+            a.mom_uy[mbase + k] = my[k];
         }
     }
 }

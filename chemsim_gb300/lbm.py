@@ -151,6 +151,13 @@ class Lattice:
                 raise ValueError("expected contiguous (h, w) float32 arrays")
         check(self._lib.lbm_read_moments_async(self._h, _f32ptr(rho), _f32ptr(ux), _f32ptr(uy)))
 
+    def step_moments_to(self, nsteps: int, rho_ptr: int, ux_ptr: int, uy_ptr: int):
+        """nsteps steps; the last writes rho/u (w*h f32 each, row-major)
+        straight to the given device or pinned-host addresses; wait with
+        readback_wait() (lbm_step_moments_to)."""
+        check(self._lib.lbm_step_moments_to(self._h, int(nsteps), ctypes.c_void_p(rho_ptr),
+                                            ctypes.c_void_p(ux_ptr), ctypes.c_void_p(uy_ptr)))
+
     def readback_wait(self):
         check(self._lib.lbm_readback_wait(self._h))
 

@@ -168,6 +168,16 @@ int lbm_read_moments(lbm_lattice* lat, float* rho, float* ux, float* uy,
  * lbm_readback_wait returns.  One readback is in flight at a time: the next
  * one's staging waits on the device for the previous host copy.            */
 int lbm_read_moments_async(lbm_lattice* lat, float* rho, float* ux, float* uy);
+/* nsteps time steps whose last one writes rho/u straight into rho, ux, uy:
+ * w*h floats each, row-major y*w+x, in memory the GPU addresses (device or
+ * managed memory, or pinned host memory from cudaHostAlloc /
+ * cudaHostRegister, which the kernel writes over the host link; pageable
+ * host memory is rejected).  Nothing is staged or copied afterwards, so the
+ * readback of a render loop costs the host-link bandwidth of the writes
+ * alone (src/main.rs:138-177 reads rho/u after every frame).  Asynchronous:
+ * lbm_readback_wait returns once the fields are written, and the handle's
+ * device moment buffers are left alone.  No reference counterpart.        */
+int lbm_step_moments_to(lbm_lattice* lat, int nsteps, float* rho, float* ux, float* uy);
 int lbm_readback_wait(lbm_lattice* lat);
 
 /* Health check (see lbm_health).  Synchronises the handle's stream.      */

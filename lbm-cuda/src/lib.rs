@@ -90,6 +90,8 @@ pub mod ffi {
                                 on_device: c_int) -> c_int;
         pub fn lbm_read_moments_async(lat: *mut LbmLattice, rho: *mut f32, ux: *mut f32,
                                       uy: *mut f32) -> c_int;
+        pub fn lbm_step_moments_to(lat: *mut LbmLattice, nsteps: c_int, rho: *mut f32, ux: *mut f32,
+                                   uy: *mut f32) -> c_int;
         pub fn lbm_readback_wait(lat: *mut LbmLattice) -> c_int;
         pub fn lbm_check(lat: *mut LbmLattice, out: *mut LbmHealth) -> c_int;
         pub fn lbm_get_time(lat: *mut LbmLattice, time: *mut f32, steps: *mut i64) -> c_int;

@@ -608,3 +608,42 @@ def test_deviation_storage_boundaries_one_step(gpu, precision, tol, edges, frame
     err = np.abs(got - want)
     assert np.all(np.isfinite(got))
     assert err.max() <= tol, f"max error {err.max():.3e} at {np.unravel_index(err.argmax(), err.shape)}"
+
+
+@pytest.mark.parametrize("precision", [F32, F16DEV])
+def test_step_moments_to_pinned_and_device_buffers(gpu, precision):
+    """lbm_step_moments_to writes the last step's rho/u straight into pinned
+    host memory or device memory, the same values lbm_step_moments leaves
+    for lbm_read_moments; pageable host memory is refused before any launch."""
+    import torch
+    spec = channel_spec(300, n_obstacles=3, r_lo=5, r_hi=12, force=1e-5, seed=6, h=70)
+    flags = spec.flags | FAST
+
+    def lattice():
+        lat = Lattice(spec.w, spec.h, spec.tau, precision, flags)
+        lat.set_force(*spec.force)
+        lat.set_geometry(spec.solid)
+        lat.init_equilibrium(spec.rho, spec.ux, spec.uy)
+        return lat
+
+    pin = [torch.zeros((spec.h, spec.w), dtype=torch.float32).pin_memory() for _ in range(3)]
+    dev = [torch.zeros((spec.h, spec.w), dtype=torch.float32, device="cuda") for _ in range(3)]
+    with lattice() as a, lattice() as b:
+        for n in (5, 1):
+            a.step_moments_to(n, *(t.data_ptr() for t in pin))
+            a.readback_wait()
+            b.step_moments(n)
+            want = b.moments()
+            for got, w in zip(pin, want):
+                assert np.array_equal(got.numpy(), w)
+        a.step_moments_to(3, *(t.data_ptr() for t in dev))
+        a.readback_wait()
+        b.step_moments(3)
+        for got, w in zip(dev, b.moments()):
+            assert np.array_equal(got.cpu().numpy(), w)
+        assert a.time() == b.time()
+        assert np.array_equal(a.get_populations(), b.get_populations())
+        pageable = np.zeros((spec.h, spec.w), np.float32)
+        with pytest.raises(lbm.LBMError):
+            a.step_moments_to(1, pageable.ctypes.data, pageable.ctypes.data, pageable.ctypes.data)
+        assert a.time() == b.time()          # refused before any step ran
