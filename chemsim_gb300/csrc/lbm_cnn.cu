@@ -364,6 +364,163 @@ dw_partial_kernel(const __nv_bfloat16* __restrict__ x, const __nv_bfloat16* __re
     if (tid < cout) bias_partial[int64_t(blockIdx.x) * cout + tid] = bacc;
 }
 
+// Weight and bias gradients of one layer on the tensor cores, partial per
+// CTA: an implicit GEMM with the pixels as the reduction dimension,
+//   D[(t, ci)][co] = sum_p x[p + off(t)][ci] g[p][co],
+// M = (tap, input channel) rows, N = output channels, K = pixels.  Both
+// operands are read from the CB8 layout as stored: there a pixel's 8
+// channels are 16 contiguous bytes, so a run of 8 pixels of one channel
+// block is a core matrix with the channels along M (or N) — the MN-major
+// form of the UMMA operands, no transposition.  Per 128-pixel row segment
+// the CTA stages, with the bulk-copy engine, the segment's pixel run of every
+// (tap, input block) (a tap's one-pixel shift is a 16-byte offset of the
+// copy's source) and of every output block of g; M-tiles of 128 rows = 16
+// (tap, block) runs, so 4 taps of 32 channels per MMA (8 taps of 16 for the
+// first layer) and the last M-tile padded with zero runs, one of which is
+// all ones: its D rows are sum_p g[p][co], the bias gradient.  The
+// accumulators stay in TMEM across the CTA's segments.
+constexpr int kDwRun = kTileM * 16;                      // bytes of one staged pixel run
+template <int CIN_B>
+constexpr int dw_groups() { return (9 * CIN_B + 1 + 15) / 16; }   // M-tiles (with the ones run)
+
+
+template <int CIN_B, int COUT_B>
+__global__ void __launch_bounds__(128)
+dw_tc_kernel(const __nv_bfloat16* __restrict__ x, const __nv_bfloat16* __restrict__ g, int B,
+             int H, int W, int cin, int cout, float* __restrict__ partial,
+             float* __restrict__ bias_partial, int* __restrict__ err) {
+    constexpr int G = dw_groups<CIN_B>();
+    constexpr int NRUNS = 16 * G;                  // A runs, padding included
+    constexpr int N = COUT_B * 8;
+    constexpr int ONES = 9 * CIN_B;                // the run of ones (first padding run)
+    extern __shared__ __align__(1024) uint8_t smem[];
+    uint8_t* sA = smem;
+    uint8_t* sB = smem + NRUNS * kDwRun;
+    uint64_t* lbar = reinterpret_cast<uint64_t*>(sB + COUT_B * kDwRun);
+    uint64_t* mbar = lbar + 1;
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(lbar + 2);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    // padding runs: zeros, the first of them ones (bf16 1.0 = 0x3F80)
+    for (int k = tid; k < (NRUNS - ONES) * kDwRun / 16; k += blockDim.x) {
+        const int run = ONES + k / (kDwRun / 16);
+        const uint32_t v = run == ONES ? 0x3F803F80u : 0u;
+        reinterpret_cast<uint4*>(sA + ONES * kDwRun)[k] = make_uint4(v, v, v, v);
+    }
+    lbmtc::fence_proxy_async_smem();
+    if (tid == 0) {
+        lbmtc::mbar_init(lbar, 1);
+        lbmtc::mbar_init(mbar, 1);
+    }
+    if (warp == 0) lbmtc::tmem_alloc(tslot, 128);
+    lbmtc::fence_before_sync();
+    __syncthreads();
+    lbmtc::fence_after_sync();
+    const uint32_t tmem = *tslot;
+
+    // MN-major operands, no swizzle: core matrices of 128 bytes (8 pixels x
+    // 8 channels); the leading byte offset is the step between core matrices
+    // along K (pixels, 128 bytes), the stride byte offset the step along M / N
+    // (one run).  (Checked against the oracle's gradients; the two offsets
+    // the other way round give wrong sums.)
+    constexpr uint32_t lbo = 128, sbo = kDwRun;
+    constexpr uint32_t idesc = lbmtc::idesc_bf16_f32(128, N) | (1u << 15) | (1u << 16);
+    const uint32_t a0 = lbmtc::smem_u32(sA), b0 = lbmtc::smem_u32(sB);
+
+    const int segs_per_row = W / kTileM;
+    const int64_t nseg = int64_t(B) * H * segs_per_row;
+    uint32_t phase = 0, acc = 0;
+    bool ok = true;
+    const uint4* xin = reinterpret_cast<const uint4*>(x);
+    const uint4* gin = reinterpret_cast<const uint4*>(g);
+    for (int64_t sgi = blockIdx.x; sgi < nseg && ok; sgi += gridDim.x) {
+        const int x0 = int(sgi % segs_per_row) * kTileM;
+        const int y = int((sgi / segs_per_row) % H);
+        const int b = int(sgi / (int64_t(segs_per_row) * H));
+        if (tid == 0) {
+            lbmtc::mbar_expect_tx(lbar, (9 * CIN_B + COUT_B) * kDwRun);
+#pragma unroll 1
+            for (int t = 0; t < 9; ++t) {
+                const int ky = t / 3, kx = t % 3;
+                for (int cb = 0; cb < CIN_B; ++cb)
+                    lbmtc::bulk_g2s(sA + (t * CIN_B + cb) * kDwRun,
+                                    xin + cb8_chunk(b, y + ky - 1, cb, x0 + kx - 1, H, W, CIN_B),
+                                    kDwRun, lbar);
+            }
+            for (int cb = 0; cb < COUT_B; ++cb)
+                lbmtc::bulk_g2s(sB + cb * kDwRun, gin + cb8_chunk(b, y, cb, x0, H, W, COUT_B), kDwRun,
+                                lbar);
+        }
+        bool staged = lbmtc::mbar_wait_bounded(lbar, phase, kWaitPolls);
+        if (!staged) {
+            if (lane == 0) atomicExch(err, 1);
+            (void)lbmtc::mbar_wait_bounded(lbar, phase, kWaitPolls);
+        }
+        staged = __syncthreads_and(staged);
+        lbmtc::fence_after_sync();
+        if (!staged) { ok = false; break; }
+        if (tid == 0) {
+#pragma unroll 1
+            for (int s = 0; s < kTileM / 16; ++s) {
+                const uint64_t bd = lbmtc::smem_desc(b0 + uint32_t(s * 256), lbo, sbo);
+#pragma unroll
+                for (int q = 0; q < G; ++q) {
+                    const uint64_t ad = lbmtc::smem_desc(a0 + uint32_t(q * 16 * kDwRun + s * 256), lbo, sbo);
+                    lbmtc::mma_bf16(tmem + uint32_t(q * N), ad, bd, idesc, acc);
+                }
+                acc = 1;
+            }
+            lbmtc::mma_commit(mbar);
+        }
+        // the MMAs read the staged tiles: wait for them before the next copy
+        bool done = lbmtc::mbar_wait_bounded(mbar, phase, kWaitPolls);
+        if (!done) {
+            if (lane == 0) atomicExch(err, 1);
+            (void)lbmtc::mbar_wait_bounded(mbar, phase, kWaitPolls);
+        }
+        ok = __syncthreads_and(done);
+        lbmtc::fence_after_sync();
+        phase ^= 1u;
+        acc = 1;
+    }
+
+    // TMEM -> partials: lane l of warp w holds D row 32 w + l of every M-tile
+    const int row = warp * 32 + lane;
+#pragma unroll
+    for (int q = 0; q < G; ++q) {
+        float v[N];
+        const uint32_t taddr = tmem + uint32_t(q * N) + (uint32_t(warp * 32) << 16);
+        if constexpr (N == 32) lbmtc::tmem_ld32(taddr, v);
+        else lbmtc::tmem_ld16(taddr, v);
+        const int run = q * 16 + row / 8, c = row % 8;
+        if (acc == 0) {
+#pragma unroll
+            for (int n = 0; n < N; ++n) v[n] = 0.f;      // no segment: nothing accumulated
+        }
+        if (run < 9 * CIN_B) {
+            const int t = run / CIN_B, ci = (run % CIN_B) * 8 + c;
+            if (ci < cin) {
+                float* dst = partial + (int64_t(blockIdx.x) * 9 * cin + t * cin + ci) * cout;
+#pragma unroll
+                for (int n = 0; n < N; ++n)
+                    if (n < cout) dst[n] = v[n];
+            }
+        } else if (run == ONES && c == 0) {
+#pragma unroll
+            for (int n = 0; n < N; ++n)
+                if (n < cout) bias_partial[int64_t(blockIdx.x) * cout + n] = v[n];
+        }
+    }
+    lbmtc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) lbmtc::tmem_dealloc(tmem, 128);
+}
+
+template <int CIN_B, int COUT_B>
+constexpr int dw_smem() {
+    return 16 * dw_groups<CIN_B>() * kDwRun + COUT_B * kDwRun + 64;
+}
+
 // grad[k] = sum over blocks of partial[block][k] (fixed order).
 __global__ void reduce_partials_kernel(const float* __restrict__ partial, int nblocks, int n,
                                        float* __restrict__ grad) {
@@ -467,6 +624,27 @@ cudaError_t launch_conv(const lbm_cnn* N, const ConvArgs& a) {
     return cudaGetLastError();
 }
 
+// Weight gradients on the tensor cores (1) or on the CUDA cores (0).
+#ifndef LBM_DW_TC
+#define LBM_DW_TC 1
+#endif
+
+template <int CIN_B, int COUT_B>
+cudaError_t launch_dw(const lbm_cnn* N, const __nv_bfloat16* x, const __nv_bfloat16* g, int B,
+                      int cin, int cout) {
+    static bool configured = false;
+    if (!configured) {
+        cudaError_t e = cudaFuncSetAttribute(dw_tc_kernel<CIN_B, COUT_B>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             dw_smem<CIN_B, COUT_B>());
+        if (e != cudaSuccess) return e;
+        configured = true;
+    }
+    dw_tc_kernel<CIN_B, COUT_B><<<N->dw_blocks, 128, dw_smem<CIN_B, COUT_B>(), N->stream>>>(
+        x, g, B, N->H, N->W, cin, cout, N->dw_partial, N->db_partial, N->err);
+    return cudaGetLastError();
+}
+
 int repack(lbm_cnn* N) {
     for (int l = 0; l < kLayers; ++l) {
         const int cbi = cbi_of(kCin[l]), no = pad16(kCout[l]);
@@ -519,16 +697,24 @@ int backward_impl(lbm_cnn* N, int B) {
         // weight and bias gradient of layer l
         const int cin = kCin[l], cout = kCout[l];
         const int pairs = 9 * cin;
-        if (l == 0)
-            dw_partial_kernel<2, 4><<<N->dw_blocks, 288, 0, N->stream>>>(
-                N->x[0], g, B, N->H, N->W, cin, cout, N->dw_partial, N->db_partial);
-        else if (l == kLayers - 1)
-            dw_partial_kernel<4, 2><<<N->dw_blocks, 288, 0, N->stream>>>(
-                N->x[l], g, B, N->H, N->W, cin, cout, N->dw_partial, N->db_partial);
-        else
-            dw_partial_kernel<4, 4><<<N->dw_blocks, 288, 0, N->stream>>>(
-                N->x[l], g, B, N->H, N->W, cin, cout, N->dw_partial, N->db_partial);
-        CNN_CUDA(cudaGetLastError());
+        cudaError_t de;
+        if (LBM_DW_TC) {
+            if (l == 0) de = launch_dw<2, 4>(N, N->x[0], g, B, cin, cout);
+            else if (l == kLayers - 1) de = launch_dw<4, 2>(N, N->x[l], g, B, cin, cout);
+            else de = launch_dw<4, 4>(N, N->x[l], g, B, cin, cout);
+        } else {
+            if (l == 0)
+                dw_partial_kernel<2, 4><<<N->dw_blocks, 288, 0, N->stream>>>(
+                    N->x[0], g, B, N->H, N->W, cin, cout, N->dw_partial, N->db_partial);
+            else if (l == kLayers - 1)
+                dw_partial_kernel<4, 2><<<N->dw_blocks, 288, 0, N->stream>>>(
+                    N->x[l], g, B, N->H, N->W, cin, cout, N->dw_partial, N->db_partial);
+            else
+                dw_partial_kernel<4, 4><<<N->dw_blocks, 288, 0, N->stream>>>(
+                    N->x[l], g, B, N->H, N->W, cin, cout, N->dw_partial, N->db_partial);
+            de = cudaGetLastError();
+        }
+        if (de != cudaSuccess) { (void)cudaGetLastError(); return cfail(LBM_ERR_CUDA, cudaGetErrorString(de)); }
         reduce_partials_kernel<<<grid_of(pairs * cout, 256), 256, 0, N->stream>>>(
             N->dw_partial, N->dw_blocks, pairs * cout, N->grads + N->off_w[l]);
         CNN_CUDA(cudaGetLastError());
