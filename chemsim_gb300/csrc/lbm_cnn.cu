@@ -75,6 +75,42 @@ struct ConvArgs {
     int* err;
 };
 
+// Epilogue of one 128-pixel tile (the CTA's 4 warps, lane = pixel): bias +
+// GELU (MODE 0), f32 NCHW output (MODE 1), or x GELU' of the previous
+// layer's pre-activation (MODE 2).
+template <int NO, int MODE>
+__device__ __forceinline__ void conv_epilogue(const ConvArgs& a, const float (&v)[NO], int b, int y,
+                                              int x) {
+    const int H = a.H, W = a.W;
+    if constexpr (MODE == 0) {
+#pragma unroll
+        for (int cb = 0; cb < NO / 8; ++cb) {
+            float z[8], gv[8];
+#pragma unroll
+            for (int c = 0; c < 8; ++c) {
+                z[c] = v[cb * 8 + c] + a.bias[cb * 8 + c];
+                gv[c] = gelu(z[c]);
+            }
+            const int64_t o = cb8_chunk(b, y, cb, x, H, W, NO / 8);
+            if (a.z_out != nullptr) reinterpret_cast<uint4*>(a.z_out)[o] = pack8_bf16(z);
+            reinterpret_cast<uint4*>(a.x_out)[o] = pack8_bf16(gv);
+        }
+    } else if constexpr (MODE == 1) {
+        for (int c = 0; c < a.nreal; ++c)
+            a.f32_out[((int64_t(b) * a.nreal + c) * H + y) * W + x] = v[c] + a.bias[c];
+    } else {
+#pragma unroll
+        for (int cb = 0; cb < NO / 8; ++cb) {
+            const int64_t o = cb8_chunk(b, y, cb, x, H, W, NO / 8);
+            float zp[8], gv[8];
+            unpack8_bf16(__ldg(reinterpret_cast<const uint4*>(a.zprev) + o), zp);
+#pragma unroll
+            for (int c = 0; c < 8; ++c) gv[c] = v[cb * 8 + c] * gelu_grad(zp[c]);
+            reinterpret_cast<uint4*>(a.x_out)[o] = pack8_bf16(gv);
+        }
+    }
+}
+
 // Dynamic shared memory of a conv CTA: A halo tile (3 rows x CBI blocks x
 // 130 pixels x 16 B; the descriptors of the 9 taps reach exactly its last
 // byte), B (weights), two mbarriers and the TMEM address slot.
@@ -167,35 +203,7 @@ conv3x3_tc_kernel(const ConvArgs a) {
     else lbmtc::tmem_ld16(taddr, v);
 
     const int x = x0 + warp * 32 + lane;
-    if (done && x < W) {
-        if constexpr (MODE == 0) {
-#pragma unroll
-            for (int cb = 0; cb < NO / 8; ++cb) {
-                float z[8], g[8];
-#pragma unroll
-                for (int c = 0; c < 8; ++c) {
-                    z[c] = v[cb * 8 + c] + a.bias[cb * 8 + c];
-                    g[c] = gelu(z[c]);
-                }
-                const int64_t o = cb8_chunk(b, y, cb, x, H, W, NO / 8);
-                if (a.z_out != nullptr) reinterpret_cast<uint4*>(a.z_out)[o] = pack8_bf16(z);
-                reinterpret_cast<uint4*>(a.x_out)[o] = pack8_bf16(g);
-            }
-        } else if constexpr (MODE == 1) {
-            for (int c = 0; c < a.nreal; ++c)
-                a.f32_out[((int64_t(b) * a.nreal + c) * H + y) * W + x] = v[c] + a.bias[c];
-        } else {
-#pragma unroll
-            for (int cb = 0; cb < NO / 8; ++cb) {
-                const int64_t o = cb8_chunk(b, y, cb, x, H, W, NO / 8);
-                float zp[8], g[8];
-                unpack8_bf16(__ldg(reinterpret_cast<const uint4*>(a.zprev) + o), zp);
-#pragma unroll
-                for (int c = 0; c < 8; ++c) g[c] = v[cb * 8 + c] * gelu_grad(zp[c]);
-                reinterpret_cast<uint4*>(a.x_out)[o] = pack8_bf16(g);
-            }
-        }
-    }
+    if (done && x < W) conv_epilogue<NO, MODE>(a, v, b, y, x);
     lbmtc::fence_before_sync();
     __syncthreads();
     if (warp == 0) lbmtc::tmem_dealloc(tmem, 32);
