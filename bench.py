@@ -564,7 +564,7 @@ def run_learned(args, torch):
     time-to-solution ratio.  Also the correction network's forward throughput
     (tcgen05 implicit-GEMM convolutions) on 8 coarse images."""
     from chemsim_gb300.learned import (CorrectionConfig, evaluate_correction, forward_throughput,
-                                       train_correction)
+                                       gradient_throughput, train_correction)
     cfg = CorrectionConfig(final_iters=args.learned_iters)
     stream = torch.cuda.Stream()
     t0 = time.perf_counter()
@@ -575,6 +575,7 @@ def run_learned(args, torch):
         net.close()
     wall = time.perf_counter() - t0
     fwd = forward_throughput(8, cfg.coarse)
+    grads = gradient_throughput(8, cfg.coarse)
     corr = ev["corrected"][0]
     return {"workload": f"fine {cfg.fine}^2 tau {cfg.tau_fine} vs coarse {cfg.coarse}^2 tau "
                         f"{cfg.tau_coarse:.4f}, {cfg.n_obstacles} obstacles, correction every "
@@ -588,7 +589,10 @@ def run_learned(args, torch):
             "time_to_solution_ratio": corr["time_to_solution_ratio"],
             "fallback_triggered_at_fine_step": corr["fallback_triggered_at_fine_step"],
             "wall_seconds": round(wall, 1),
-            "forward": fwd}
+            "forward": fwd,
+            "gradients": dict(grads, note="lbm_cnn_gradients: forward keeping the pre-activations, "
+                                           "loss, input gradients and weight gradients, all on "
+                                           "tcgen05; each call waits for its loss")}
 
 
 def run_large(args, torch):

@@ -463,12 +463,31 @@ def forward_throughput(images: int = 8, side: int = 512, reps: int = 20) -> dict
             "algorithmic_gflop": round(flops / 1e9, 2), "tflops": round(flops / secs / 1e12, 1)}
 
 
+def gradient_throughput(images: int = 8, side: int = 512, reps: int = 10) -> dict:
+    """Times lbm_cnn_gradients (forward with the pre-activations kept, loss,
+    input gradients and the tcgen05 weight gradients) on `images` random
+    images of side x side; each call waits for its loss."""
+    import torch
+    with CorrectionNet(side, side, images, seed=1) as net:
+        x = torch.randn((images, 4, side, side), device="cuda")
+        t = torch.randn((images, 9, side, side), device="cuda") * 0.1
+        torch.cuda.synchronize()
+        for _ in range(2):
+            net.gradients(x, t)
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            net.gradients(x, t)
+        secs = (time.perf_counter() - t0) / reps
+    return {"images": images, "side": side, "ms": round(secs * 1e3, 3)}
+
+
 if __name__ == "__main__":
-    # python -m chemsim_gb300.learned forward [images] [side]
+    # python -m chemsim_gb300.learned forward|gradients [images] [side]
     import json
     import sys
-    if len(sys.argv) < 2 or sys.argv[1] != "forward":
-        sys.exit("usage: python -m chemsim_gb300.learned forward [images] [side]")
+    if len(sys.argv) < 2 or sys.argv[1] not in ("forward", "gradients"):
+        sys.exit("usage: python -m chemsim_gb300.learned forward|gradients [images] [side]")
     n = int(sys.argv[2]) if len(sys.argv) > 2 else 8
     side = int(sys.argv[3]) if len(sys.argv) > 3 else 512
-    print(json.dumps(forward_throughput(n, side)))
+    fn = forward_throughput if sys.argv[1] == "forward" else gradient_throughput
+    print(json.dumps(fn(n, side)))
