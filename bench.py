@@ -531,7 +531,7 @@ def run_batch(args, torch):
     b.autotune(cache)
     tune_s = time.perf_counter() - t0
     with open(cache) as fh:
-        tiles = {str(e["class"]): e["V"] for e in json.load(fh)["lbm_batch_autotune"]}
+        tuned = json.load(fh)["lbm_batch_autotune"][-1]
     b.step(args.warmup)
     b.synchronize()
     start = torch.cuda.Event(enable_timing=True)
@@ -542,6 +542,7 @@ def run_batch(args, torch):
     end.synchronize()
     secs = start.elapsed_time(end) / 1e3
     health = [m.health() for m in b.members[:8]]
+    tile = b.tile()
     b.close()
     peak, _ = measured_peak_gbs()
     gbs = (BYTES_F32 + BYTES_MASK) * cells * args.batch_steps / secs / 1e9
@@ -550,8 +551,9 @@ def run_batch(args, torch):
             "cells": cells, "steps": args.batch_steps, "mlups": round(cells * args.batch_steps / secs / 1e6, 1),
             "achieved_gbs": round(gbs, 1), "frac": round(gbs / peak, 4),
             "ms_per_step": round(secs / args.batch_steps * 1e3, 4), "autotune_s": round(tune_s, 2),
-            "tiles_cells_per_thread_by_width_class": tiles,
-            "launches_per_step": "one per non-empty (tile width, path) list",
+            "tile_cells_per_thread": tile,
+            "autotune_mlups": {"2": tuned["mlups_v2"], "4": tuned["mlups_v4"]},
+            "launches_per_step": 1,
             "stable": all(not h["unstable"] for h in health)}
 
 

@@ -113,6 +113,8 @@ SIGNATURES = {
     "lbm_batch_step": (_i32, [_vp, _i32]),
     "lbm_batch_synchronize": (_i32, [_vp]),
     "lbm_batch_set_stream": (_i32, [_vp, _vp]),
+    "lbm_batch_set_tile": (_i32, [_vp, _i32]),
+    "lbm_batch_tile": (_i32, [_vp, ctypes.POINTER(_i32)]),
     "lbm_batch_autotune": (_i32, [_vp, ctypes.c_char_p, _i32]),
     "lbm_read_moments_async": (_i32, [_vp, _vp, _vp, _vp]),
     "lbm_step_moments_to": (_i32, [_vp, _i32, _vp, _vp, _vp]),

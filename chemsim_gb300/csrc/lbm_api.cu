@@ -212,6 +212,7 @@ int ensure_staging(lbm_lattice* L, size_t bytes) {
 #ifndef LBM_LINKS_IN_GRID
 #define LBM_LINKS_IN_GRID 1
 #endif
+
 // Recomputes the per-(row, warp tile) boundary/solid flags for the current
 // tile width and geometry.
 int refresh_tiles(lbm_lattice* L) {
@@ -231,11 +232,12 @@ int refresh_tiles(lbm_lattice* L) {
     LBM_CUDA(cudaMemcpyAsync(flags.data(), L->tflags, flags.size(), cudaMemcpyDeviceToHost,
                              L->stream));
     LBM_CUDA(cudaStreamSynchronize(L->stream));
-    // 16-bit storage at 8 cells per thread: tiles flagged 3 take the interior
-    // path with per-lane link masks (computed here), so only tiles flagged 1
-    // are listed.
-    const bool in_grid = LBM_LINKS_IN_GRID && L->has_solid && L->vcells == 8 &&
-                         (L->precision == LBM_F16DEV || L->precision == LBM_BF16DEV);
+    // 16-bit storage at 8 cells per thread and f32 at any tile width: tiles
+    // flagged 3 take the interior path with per-lane link masks (computed
+    // here), so only tiles flagged 1 are listed.
+    const bool dev16 = L->precision == LBM_F16DEV || L->precision == LBM_BF16DEV;
+    const bool in_grid = LBM_LINKS_IN_GRID && L->has_solid &&
+                         ((dev16 && L->vcells == 8) || (LBM_LINKS_F32 && L->precision == LBM_F32));
     if (in_grid) {
         const size_t need = size_t(n) * 32;
         if (need > L->links_cap) {

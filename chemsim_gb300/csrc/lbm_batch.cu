@@ -2,12 +2,14 @@
 //
 // A batch owns n ordinary lattices (lbm_lattice handles, so every
 // single-lattice entry point works on a member) and advances all of them by
-// one persistent launch per time step: the grid is sized to fill the GPU
-// once, and each warp walks the list of work items (member, row, warp tile)
-// of all members, running the same interior / general step code as a single
-// lattice, so a member's results do not depend on whether it was stepped
-// alone or in a batch.  Runs of steps replay a captured CUDA graph.  The
-// autotuner picks the tile width (cells per thread) per width class.
+// one launch per time step.  The launch covers a list of work items, one per
+// warp: (member, row, warp tile) of every member, general items first, then
+// each member in blocks of 8 rows of one tile column, so the 8 warps of a CTA
+// share the rows they pull from.  Each warp runs the same interior / general /
+// link-mask step code as a single lattice, so a member's results do not depend
+// on whether it was stepped alone or in a batch.  Runs of steps replay a
+// captured CUDA graph.  The autotuner picks the batch's tile width (2 or 4
+// cells per thread, one kernel each).
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -21,8 +23,6 @@ using namespace lbmk;
 
 struct lbm_batch_member_dev {
     StepArgs<float> a[2];   // from the member's buffer at build time (0) or the other (1)
-    int V;                  // cells per thread
-    int rows;               // warp rows per task
 };
 
 struct lbm_batch {
@@ -30,15 +30,14 @@ struct lbm_batch {
     std::vector<uint64_t> built_version;
     std::vector<int> built_cur;
     lbm_batch_member_dev* d_members = nullptr;
-    uint2* d_tasks = nullptr;         // work items (member, row << 12 | tile), 4 lists
-    int list_off[7] = {0, 0, 0, 0, 0, 0, 0};
+    uint2* d_tasks = nullptr;         // work items (member | kind << 24, row << 12 | tile)
     int ntasks = 0;
     size_t tasks_cap = 0;
     int par = 0;                      // steps since the table was built, mod 2
     bool built = false;
     int frame = 0, fast = 1;
-    int grid[6] = {0, 0, 0, 0, 0, 0};  // per list: resident blocks of its kernel x SMs
-    int grid_fused = 0;               // the same for the fused kernel
+    int V = 4;                        // cells per thread of every member in batch steps
+    int resident[2] = {0, 0};         // resident warps of the V = 2 and V = 4 kernels, whole GPU
     cudaStream_t own = nullptr, stream = nullptr;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     int dev = 0;
@@ -49,133 +48,68 @@ namespace {
 
 constexpr int kTaskWarps = 8;
 constexpr int kBatchGraphSteps = 16;
+constexpr int kDefaultV = 4;
 
-// Blocks of 8 warps per SM: 3 for the narrow-tile interior kernel, 2 (128
-// registers a thread) for the others.  The member's arguments are read from memory,
-// so collision constants live in registers.
-#ifndef LBM_BATCH_MIN_BLOCKS
-#define LBM_BATCH_MIN_BLOCKS 3
-#endif
+// Item kinds (bits 24-31 of the item's first word).
+enum : uint32_t { kGeneral = 0, kWrap = 1, kInterior = 2, kLinks = 3 };
+
 #ifndef LBM_BATCH_PREFETCH
 #define LBM_BATCH_PREFETCH 1
 #endif
-// 1: every step is one launch of the fused kernel over all items; 0 (the
-// default): one launch per non-empty list, each of its own kernel.  A/B on
-// one GB300 (512 members, 154 M cells, autotuned): fused 0.566 of the copy
-// bandwidth, lists 0.680.  The fused kernel takes the registers of its
-// largest path (the general step, 128 a thread), so the lean items, which
-// need 80, run at two thirds of their occupancy.
-#ifndef LBM_BATCH_FUSED
-#define LBM_BATCH_FUSED 0
-#endif
 
-// One warp = one work item; a warp walks its item list with a stride of the
-// whole grid, fetching the next item before it works on the current one, and
-// reads its member's step arguments straight from the (L1/L2-resident) member
-// table, so warps never wait for one another.  Item word x = member index,
-// word y = row << 12 | tile.  Each kernel carries one code path (the items
-// are split by tile width and by the tile flag: PATH 1 = the full boundary /
-// solid treatment, 2 = the interior step that wraps at periodic edges, 0 =
-// the lean interior step), which keeps the instruction working set of an SM
-// small.
-template <int V, int FRAME, bool FAST, int PATH>
-__global__ void __launch_bounds__(256, (PATH == 1 || V == 4) ? 2 : LBM_BATCH_MIN_BLOCKS)
+// L2 prefetch of the rows item q pulls, one plane a lane (the range is
+// clipped to the row's pitch, so it stays inside the member's buffer).
+template <int V, int FRAME>
+__device__ __forceinline__ void prefetch_item(const lbm_batch_member_dev* __restrict__ members,
+                                              const uint2* __restrict__ items, int nitems, int q,
+                                              int parity, int lane) {
+    if (!LBM_BATCH_PREFETCH || lane >= 9 || q >= nitems) return;
+    const uint2 next = items[q];
+    const StepArgs<float>& an = members[next.x & 0xffffffu].a[parity];
+    const int ys = int(next.y >> 12) - DROW(FRAME, lane);
+    const int x0 = int(next.y & 4095u) * 32 * V;
+    if (ys >= 0 && ys < an.h) {
+        const int n = min(32 * V, an.pitch - x0);
+        const float* p = static_cast<const float*>(an.src) + lane * an.plane + int64_t(ys) * an.pitch + x0;
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" :: "l"(p), "r"(n * 4) : "memory");
+    }
+}
+
+// One warp = one work item: the kind dispatch is warp-uniform.  After its own
+// item the warp prefetches into L2 the rows of the item about one wave of
+// resident warps ahead (after, not before: the prefetch first reads that
+// item and its member's arguments).  Registers: V = 4 at 3 CTAs of 8 warps
+// per SM (80 a thread), V = 2 at 4 (64); the general path spills a little at
+// both, the interior paths fit.
+template <int V, int FRAME, bool FAST>
+__global__ void __launch_bounds__(256, V == 2 ? 4 : 3)
 lbm_batch_kernel(const lbm_batch_member_dev* __restrict__ members, const uint2* __restrict__ items,
-                 int nitems, int parity) {
+                 int nitems, int parity, int pf) {
     const int lane = threadIdx.x;
-    const int warps = gridDim.x * blockDim.y;
-    int it = blockIdx.x * blockDim.y + threadIdx.y;
-    uint2 item = it < nitems ? items[it] : make_uint2(0u, 0u);
-    for (; it < nitems; it += warps) {
-        const uint2 next = it + warps < nitems ? items[it + warps] : make_uint2(0u, 0u);
-        if (LBM_BATCH_PREFETCH && lane < 9 && it + warps < nitems) {
-            // L2 prefetch of the rows the next item pulls, one plane a lane
-            // (the range is clipped to the row's pitch, so it stays inside
-            // the member's buffer)
-            const StepArgs<float>& an = members[next.x & 0xffffffu].a[parity];
-            const int ys = int(next.y >> 12) - DROW(FRAME, lane);
-            const int x0 = int(next.y & 4095u) * 32 * V;
-            if (ys >= 0 && ys < an.h) {
-                const int n = min(32 * V, an.pitch - x0);
-                const float* p = static_cast<const float*>(an.src) + lane * an.plane +
-                                 int64_t(ys) * an.pitch + x0;
-                asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" :: "l"(p), "r"(n * 4) : "memory");
-            }
-        }
-        const StepArgs<float>& a = members[item.x & 0xffffffu].a[parity];
-        const int y = int(item.y >> 12), tile = int(item.y & 4095u);
-        if constexpr (PATH == 1) step_general<float, V, FRAME, FAST>(a, y, tile, lane);
-        else if constexpr (PATH == 2) step_interior_wrap<float, V, FRAME, FAST>(a, y, (tile * 32 + lane) * V, lane);
-        else step_interior<float, V, FRAME, FAST>(a, y, (tile * 32 + lane) * V, lane);
-        item = next;
+    const int it = blockIdx.x * blockDim.y + threadIdx.y;
+    if (it >= nitems) return;
+    const uint2 item = items[it];
+    const StepArgs<float>& a = members[item.x & 0xffffffu].a[parity];
+    const int y = int(item.y >> 12), tile = int(item.y & 4095u);
+    const int x0 = (tile * 32 + lane) * V;
+    switch (item.x >> 24) {      // warp-uniform
+        case kGeneral: step_general<float, V, FRAME, FAST>(a, y, tile, lane); break;
+        case kWrap: step_interior_wrap<float, V, FRAME, FAST>(a, y, x0, lane); break;
+        case kInterior: step_interior<float, V, FRAME, FAST>(a, y, x0, lane); break;
+        default: step_interior<float, V, FRAME, FAST, false, true>(a, y, x0, lane, tile); break;
     }
+    prefetch_item<V, FRAME>(members, items, nitems, it + pf, parity, lane);
 }
 
-// All item kinds in one persistent kernel: item word x carries the member
-// index in its low 24 bits and the list (tile width and path) in bits 24-26,
-// and the warp dispatches on it, so a step is one launch.  Lists stay in
-// order (general items first, so their longer latency overlaps the rest).
-template <int FRAME, bool FAST>
-__global__ void __launch_bounds__(256, 2)
-lbm_batch_fused_kernel(const lbm_batch_member_dev* __restrict__ members,
-                       const uint2* __restrict__ items, int nitems, int parity) {
-    const int lane = threadIdx.x;
-    const int warps = gridDim.x * blockDim.y;
-    int it = blockIdx.x * blockDim.y + threadIdx.y;
-    uint2 item = it < nitems ? items[it] : make_uint2(0u, 0u);
-    for (; it < nitems; it += warps) {
-        const uint2 next = it + warps < nitems ? items[it + warps] : make_uint2(0u, 0u);
-        const int m = int(item.x & 0xffffffu), k = int(item.x >> 24);
-        if (LBM_BATCH_PREFETCH && lane < 9 && it + warps < nitems) {
-            const int nk = int(next.x >> 24), nv = nk < 3 ? 2 : 4;
-            const StepArgs<float>& an = members[next.x & 0xffffffu].a[parity];
-            const int ys = int(next.y >> 12) - DROW(FRAME, lane);
-            const int x0 = int(next.y & 4095u) * 32 * nv;
-            if (ys >= 0 && ys < an.h) {
-                const int n = min(32 * nv, an.pitch - x0);
-                const float* p = static_cast<const float*>(an.src) + lane * an.plane +
-                                 int64_t(ys) * an.pitch + x0;
-                asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" :: "l"(p), "r"(n * 4) : "memory");
-            }
-        }
-        const StepArgs<float>& a = members[m].a[parity];
-        const int y = int(item.y >> 12), tile = int(item.y & 4095u);
-        switch (k) {     // warp-uniform
-            case 0: step_general<float, 2, FRAME, FAST>(a, y, tile, lane); break;
-            case 1: step_interior_wrap<float, 2, FRAME, FAST>(a, y, (tile * 32 + lane) * 2, lane); break;
-            case 2: step_interior<float, 2, FRAME, FAST>(a, y, (tile * 32 + lane) * 2, lane); break;
-            case 3: step_general<float, 4, FRAME, FAST>(a, y, tile, lane); break;
-            case 4: step_interior_wrap<float, 4, FRAME, FAST>(a, y, (tile * 32 + lane) * 4, lane); break;
-            default: step_interior<float, 4, FRAME, FAST>(a, y, (tile * 32 + lane) * 4, lane); break;
-        }
-        item = next;
+using BatchKernel = void (*)(const lbm_batch_member_dev*, const uint2*, int, int, int);
+
+BatchKernel pick_kernel(int V, int frame, int fast) {
+    if (V == 2) {
+        if (frame) return fast ? lbm_batch_kernel<2, 1, true> : lbm_batch_kernel<2, 1, false>;
+        return fast ? lbm_batch_kernel<2, 0, true> : lbm_batch_kernel<2, 0, false>;
     }
-}
-
-using BatchKernel = void (*)(const lbm_batch_member_dev*, const uint2*, int, int);
-
-BatchKernel pick_fused(int frame, int fast) {
-    if (frame) return fast ? lbm_batch_fused_kernel<1, true> : lbm_batch_fused_kernel<1, false>;
-    return fast ? lbm_batch_fused_kernel<0, true> : lbm_batch_fused_kernel<0, false>;
-}
-
-template <int V, int PATH>
-BatchKernel pick_kernel_v(int frame, int fast) {
-    if (frame) return fast ? lbm_batch_kernel<V, 1, true, PATH> : lbm_batch_kernel<V, 1, false, PATH>;
-    return fast ? lbm_batch_kernel<V, 0, true, PATH> : lbm_batch_kernel<V, 0, false, PATH>;
-}
-
-// List k = 3 * (V == 4) + j with j = 0 general, 1 periodic edge, 2 lean.
-constexpr int kLists = 6;
-BatchKernel pick_kernel(int list, int frame, int fast) {
-    switch (list) {
-        case 0: return pick_kernel_v<2, 1>(frame, fast);
-        case 1: return pick_kernel_v<2, 2>(frame, fast);
-        case 2: return pick_kernel_v<2, 0>(frame, fast);
-        case 3: return pick_kernel_v<4, 1>(frame, fast);
-        case 4: return pick_kernel_v<4, 2>(frame, fast);
-        default: return pick_kernel_v<4, 0>(frame, fast);
-    }
+    if (frame) return fast ? lbm_batch_kernel<4, 1, true> : lbm_batch_kernel<4, 1, false>;
+    return fast ? lbm_batch_kernel<4, 0, true> : lbm_batch_kernel<4, 0, false>;
 }
 
 int bfail(int code, const std::string& msg) { return lattice_fail(code, msg); }
@@ -198,9 +132,14 @@ void drop_graphs(lbm_batch* B) {
     }
 }
 
-// (Re)builds the device member table and the task list when a member changed.
+// (Re)builds the device member table and the item list when a member changed.
+// Members step at the batch's tile width: a member set to another width (by
+// lbm_set_tile) is set back to it here.
 int ensure_table(lbm_batch* B) {
     const int n = int(B->members.size());
+    for (lbm_lattice* L : B->members)
+        if (L->vcells != B->V)
+            if (int rc = lbm_set_tile(L, B->V, L->rows)) return rc;
     bool changed = !B->built;
     for (int i = 0; i < n && !changed; ++i) {
         const lbm_lattice* L = B->members[i];
@@ -208,35 +147,34 @@ int ensure_table(lbm_batch* B) {
     }
     if (!changed) return LBM_OK;
     std::vector<lbm_batch_member_dev> host(n);
-    std::vector<uint2> lists[kLists];
+    std::vector<uint2> general, rest;
     std::vector<uint8_t> flags;
     for (int i = 0; i < n; ++i) {
         lbm_lattice* L = B->members[i];
         host[i].a[0] = lattice_args<float>(L, L->cur, false);
         host[i].a[1] = lattice_args<float>(L, L->cur ^ 1, false);
-        host[i].V = L->vcells;
-        host[i].rows = L->rows;
         B->built_version[i] = L->version;
         B->built_cur[i] = L->cur;
         flags.resize(size_t(L->h) * L->ntiles);
         BATCH_CUDA(cudaMemcpyAsync(flags.data(), L->tflags, flags.size(), cudaMemcpyDeviceToHost,
                                    B->stream));
         BATCH_CUDA(cudaStreamSynchronize(B->stream));
-        const int vbase = L->vcells == 2 ? 0 : 3;
-        for (int r = 0; r < L->h; ++r)
-            for (int t = 0; t < L->ntiles; ++t) {
-                const uint8_t fl = flags[size_t(r) * L->ntiles + t];
-                const int j = (fl & 1) ? 0 : (fl == 2 ? 1 : 2);     // 1, 3: general
-                lists[vbase + j].push_back(make_uint2(uint32_t(i) | (uint32_t(vbase + j) << 24),
-                                                      (uint32_t(r) << 12) | uint32_t(t)));
-            }
+        for (int r0 = 0; r0 < L->h; r0 += kTaskWarps)
+            for (int t = 0; t < L->ntiles; ++t)
+                for (int r = r0; r < std::min(L->h, r0 + kTaskWarps); ++r) {
+                    const uint8_t fl = flags[size_t(r) * L->ntiles + t];
+                    // flag 3 (solids nearby, no lattice edge in reach) runs the
+                    // interior code with link masks when the member has them
+                    const uint32_t kind = fl == 0 ? kInterior : fl == 2 ? kWrap
+                                        : (fl == 3 && L->use_links) ? kLinks : kGeneral;
+                    const uint2 item = make_uint2(uint32_t(i) | (kind << 24),
+                                                  (uint32_t(r) << 12) | uint32_t(t));
+                    (kind == kGeneral ? general : rest).push_back(item);
+                }
     }
-    std::vector<uint2> tasks;
-    for (int k = 0; k < kLists; ++k) {
-        B->list_off[k] = int(tasks.size());
-        tasks.insert(tasks.end(), lists[k].begin(), lists[k].end());
-    }
-    B->list_off[kLists] = int(tasks.size());
+    // general items first: their longer latency overlaps the rest
+    std::vector<uint2> tasks(general);
+    tasks.insert(tasks.end(), rest.begin(), rest.end());
     if (!B->d_members) BATCH_CUDA(cudaMalloc(&B->d_members, sizeof(lbm_batch_member_dev) * n));
     BATCH_CUDA(cudaMemcpyAsync(B->d_members, host.data(), sizeof(lbm_batch_member_dev) * n,
                                cudaMemcpyHostToDevice, B->stream));
@@ -247,8 +185,9 @@ int ensure_table(lbm_batch* B) {
         BATCH_CUDA(cudaMalloc(&B->d_tasks, sizeof(uint2) * tasks.size()));
         B->tasks_cap = tasks.size();
     }
-    BATCH_CUDA(cudaMemcpyAsync(B->d_tasks, tasks.data(), sizeof(uint2) * tasks.size(),
-                               cudaMemcpyHostToDevice, B->stream));
+    if (!tasks.empty())
+        BATCH_CUDA(cudaMemcpyAsync(B->d_tasks, tasks.data(), sizeof(uint2) * tasks.size(),
+                                   cudaMemcpyHostToDevice, B->stream));
     BATCH_CUDA(cudaStreamSynchronize(B->stream));
     B->ntasks = int(tasks.size());
     B->par = 0;
@@ -257,26 +196,14 @@ int ensure_table(lbm_batch* B) {
     return LBM_OK;
 }
 
-// One step: for each tile width, the general items, then the periodic-edge
-// and the lean interior items, one launch per non-empty list.
+// One step: one launch, one warp per item.
 cudaError_t launch(lbm_batch* B, int parity) {
-    if (LBM_BATCH_FUSED) {
-        if (B->ntasks == 0) return cudaSuccess;
-        const int grid = std::min(B->grid_fused, (B->ntasks + kTaskWarps - 1) / kTaskWarps);
-        pick_fused(B->frame, B->fast)<<<grid, dim3(32, kTaskWarps), 0, B->stream>>>(
-            B->d_members, B->d_tasks, B->ntasks, parity);
-        return cudaGetLastError();
-    }
-    for (int k = 0; k < kLists; ++k) {
-        const int n = B->list_off[k + 1] - B->list_off[k];
-        if (n == 0) continue;
-        const int grid = std::min(B->grid[k], (n + kTaskWarps - 1) / kTaskWarps);
-        pick_kernel(k, B->frame, B->fast)<<<grid, dim3(32, kTaskWarps), 0, B->stream>>>(
-            B->d_members, B->d_tasks + B->list_off[k], n, parity);
-        cudaError_t e = cudaGetLastError();
-        if (e != cudaSuccess) return e;
-    }
-    return cudaSuccess;
+    if (B->ntasks == 0) return cudaSuccess;
+    const int grid = (B->ntasks + kTaskWarps - 1) / kTaskWarps;
+    const int pf = std::max(1, B->resident[B->V == 4]);
+    pick_kernel(B->V, B->frame, B->fast)<<<grid, dim3(32, kTaskWarps), 0, B->stream>>>(
+        B->d_members, B->d_tasks, B->ntasks, parity, pf);
+    return cudaGetLastError();
 }
 
 int ensure_graph(lbm_batch* B) {
@@ -311,9 +238,9 @@ int width_class(int w) {
     return 4;
 }
 
-// Candidate tiles (cells per thread; the batch kernel's warp tile is 32 x
-// that wide).  Rows per block only shapes a member's own launches.
-const int kCandidates[][1] = {{2}, {4}};
+// Candidate tile widths (cells per thread; the batch kernel's warp tile is
+// 32 x that wide), one kernel each.
+const int kCandidates[2] = {2, 4};
 
 }  // namespace
 
@@ -329,6 +256,7 @@ int lbm_batch_create(int n, const lbm_desc* descs, int flags, lbm_batch** out) {
     lbm_batch* B = new lbm_batch();
     B->frame = (flags & LBM_FRAME_XY) ? 1 : 0;
     B->fast = (flags & LBM_FAST) ? 1 : 0;
+    B->V = kDefaultV;
     auto cleanup = [&](int rc) { lbm_batch_destroy(B); return rc; };
     if (cudaGetDevice(&B->dev) != cudaSuccess) return cleanup(bfail(LBM_ERR_CUDA, "no device"));
     for (int i = 0; i < n; ++i) {
@@ -356,22 +284,14 @@ int lbm_batch_create(int n, const lbm_desc* descs, int flags, lbm_batch** out) {
     // batch steps without any host synchronisation.
     for (lbm_lattice* L : B->members)
         if (int rc = lbm_set_stream(L, B->stream)) return cleanup(rc);
-    // Each list's persistent grid is exactly one wave of its own kernel: the
-    // kernels differ in registers (2 or 3 resident blocks per SM), and a
-    // second partial wave would leave SMs idle at the end of the launch.
+    // Resident warps of each kernel on the whole GPU: the prefetch distance.
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, B->dev);
-    for (int k = 0; k < kLists; ++k) {
+    for (int q = 0; q < 2; ++q) {
         int per_sm = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pick_kernel(k, B->frame, B->fast),
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pick_kernel(2 + 2 * q, B->frame, B->fast),
                                                       32 * kTaskWarps, 0);
-        B->grid[k] = std::max(1, sms) * std::max(1, per_sm);
-    }
-    {
-        int per_sm = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pick_fused(B->frame, B->fast),
-                                                      32 * kTaskWarps, 0);
-        B->grid_fused = std::max(1, sms) * std::max(1, per_sm);
+        B->resident[q] = std::max(1, sms) * std::max(1, per_sm) * kTaskWarps;
     }
     *out = B;
     return LBM_OK;
@@ -440,6 +360,21 @@ int lbm_batch_set_stream(lbm_batch* B, void* stream) {
     return LBM_OK;
 }
 
+int lbm_batch_set_tile(lbm_batch* B, int cells_per_thread) {
+    if (!B) return bfail(LBM_ERR_INVALID_ARGUMENT, "null batch");
+    if (cells_per_thread != 2 && cells_per_thread != 4)
+        return bfail(LBM_ERR_INVALID_ARGUMENT, "a batch steps with 2 or 4 cells per thread");
+    BATCH_CUDA(cudaStreamSynchronize(B->stream));
+    B->V = cells_per_thread;
+    return ensure_table(B);
+}
+
+int lbm_batch_tile(lbm_batch* B, int* cells_per_thread) {
+    if (!B || !cells_per_thread) return bfail(LBM_ERR_INVALID_ARGUMENT, "null argument");
+    *cells_per_thread = B->V;
+    return LBM_OK;
+}
+
 int lbm_batch_autotune(lbm_batch* B, const char* cache_path, int steps_per_trial) {
     if (!B) return bfail(LBM_ERR_INVALID_ARGUMENT, "null batch");
     if (steps_per_trial <= 0) steps_per_trial = 24;
@@ -449,11 +384,10 @@ int lbm_batch_autotune(lbm_batch* B, const char* cache_path, int steps_per_trial
     std::snprintf(keybuf, sizeof(keybuf), "%s|f32|%s|%s", prop.name, B->frame ? "xy" : "ref",
                   B->fast ? "fast" : "strict");
     const std::string key(keybuf);
-    const int ncand = int(sizeof(kCandidates) / sizeof(kCandidates[0]));
-    int choice[5][2];
-    bool have[5] = {false, false, false, false, false};
-    // cached choices: one JSON object per line, {"key": "...", "class": c, "V": v, "rows": r, ...}
+    // Cache: one JSON object per line, {"key": "...", "V": v, ...}; a line of
+    // this key gives the choice, lines of other keys are kept.
     std::vector<std::string> kept;
+    int cached = 0;
     if (cache_path) {
         if (FILE* fh = std::fopen(cache_path, "r")) {
             char line[1024];
@@ -463,46 +397,36 @@ int lbm_batch_autotune(lbm_batch* B, const char* cache_path, int steps_per_trial
                 k += 8;
                 const char* ke = std::strchr(k, '"');
                 if (!ke) continue;
-                std::string lk(k, ke - k);
-                int c = -1, v = 0, r = 0;
-                const char* pc = std::strstr(line, "\"class\": ");
+                const std::string lk(k, ke - k);
                 const char* pv = std::strstr(line, "\"V\": ");
-                const char* pr = std::strstr(line, "\"rows\": ");
-                if (pc) c = std::atoi(pc + 9);
-                if (pv) v = std::atoi(pv + 5);
-                if (pr) r = std::atoi(pr + 8);
+                const int v = pv ? std::atoi(pv + 5) : 0;
                 std::string body(line);
                 while (!body.empty() && (body.back() == '\n' || body.back() == ',' || body.back() == ' '))
                     body.pop_back();
-                if (lk == key && c >= 0 && c < 5 && (v == 2 || v == 4) && (r == 1 || r == 2 || r == 4 || r == 8)) {
-                    choice[c][0] = v;
-                    choice[c][1] = r;
-                    have[c] = true;
-                } else if (body.find("\"key\"") != std::string::npos) {
-                    kept.push_back(body);
-                }
+                if (lk == key && (v == 2 || v == 4)) cached = v;
+                else kept.push_back(body);
             }
             std::fclose(fh);
         }
     }
-    bool needed[5] = {false, false, false, false, false};
-    for (lbm_lattice* L : B->members) needed[width_class(L->w)] = true;
-    std::vector<std::string> timed;
+    if (cached) {
+        B->V = cached;
+        return ensure_table(B);
+    }
+    // Time both widths on each width class's members in turn, through a
+    // non-owning view of them, with their state saved first and restored
+    // afterwards (one class at a time bounds the saved copy), and sum.
+    double total_ms[2] = {0.0, 0.0}, cells = 0.0;
     for (int c = 0; c < 5; ++c) {
-        if (!needed[c] || have[c]) continue;
-        // Time the class's own members through a non-owning view of them,
-        // with their state saved first and restored afterwards.
         lbm_batch view;
         view.owns = false;
         view.frame = B->frame;
         view.fast = B->fast;
-        std::copy(B->grid, B->grid + kLists, view.grid);
-        view.grid_fused = B->grid_fused;
+        std::copy(B->resident, B->resident + 2, view.resident);
         view.stream = B->stream;
         view.dev = B->dev;
         struct Saved { void* f; int cur; float time; int64_t steps; int v, rows; };
         std::vector<Saved> saved;
-        double cells = 0.0;
         int rc = LBM_OK;
         for (lbm_lattice* L : B->members) {
             if (width_class(L->w) != c) continue;
@@ -511,21 +435,25 @@ int lbm_batch_autotune(lbm_batch* B, const char* cache_path, int steps_per_trial
             cudaError_t e = cudaMallocAsync(&sv.f, bytes, B->stream);
             if (e == cudaSuccess)
                 e = cudaMemcpyAsync(sv.f, L->buf[L->cur], bytes, cudaMemcpyDeviceToDevice, B->stream);
-            if (e != cudaSuccess) { rc = bfail(LBM_ERR_CUDA, cudaGetErrorString(e)); (void)cudaGetLastError(); break; }
+            if (e != cudaSuccess) {
+                if (sv.f) cudaFreeAsync(sv.f, B->stream);
+                rc = bfail(LBM_ERR_CUDA, cudaGetErrorString(e));
+                (void)cudaGetLastError();
+                break;
+            }
             saved.push_back(sv);
             view.members.push_back(L);
             view.built_version.push_back(~uint64_t(0));
             view.built_cur.push_back(0);
             cells += double(L->w) * L->h;
         }
-        float best = 1e30f;
-        int bv = 4;
         cudaEvent_t e0 = nullptr, e1 = nullptr;
-        if (!rc) { cudaEventCreate(&e0); cudaEventCreate(&e1); }
-        for (int q = 0; q < ncand && !rc; ++q) {
-            for (lbm_lattice* L : view.members)
-                if ((rc = lbm_set_tile(L, kCandidates[q][0], L->rows))) break;
-            if (!rc) rc = lbm_batch_step(&view, 4);
+        if (!rc && !view.members.empty()) { cudaEventCreate(&e0); cudaEventCreate(&e1); }
+        for (int q = 0; q < 2 && !rc && !view.members.empty(); ++q) {
+            view.V = kCandidates[q];
+            view.built = false;
+            drop_graphs(&view);
+            rc = lbm_batch_step(&view, 4);
             if (rc) break;
             cudaEventRecord(e0, B->stream);
             rc = lbm_batch_step(&view, steps_per_trial);
@@ -533,7 +461,7 @@ int lbm_batch_autotune(lbm_batch* B, const char* cache_path, int steps_per_trial
             if (!rc && cudaEventSynchronize(e1) != cudaSuccess) rc = bfail(LBM_ERR_CUDA, "autotune timing failed");
             float ms = 0.f;
             if (!rc) cudaEventElapsedTime(&ms, e0, e1);
-            if (!rc && ms < best) { best = ms; bv = kCandidates[q][0]; }
+            total_ms[q] += ms;
         }
         if (e0) cudaEventDestroy(e0);
         if (e1) cudaEventDestroy(e1);
@@ -558,42 +486,24 @@ int lbm_batch_autotune(lbm_batch* B, const char* cache_path, int steps_per_trial
         drop_graphs(&view);
         if (cudaStreamSynchronize(B->stream) != cudaSuccess && !rc) rc = bfail(LBM_ERR_CUDA, "autotune restore");
         if (rc) return rc;
-        choice[c][0] = bv;
-        choice[c][1] = 4;
-        have[c] = true;
+    }
+    const int best = total_ms[0] < total_ms[1] ? 0 : 1;
+    B->V = kCandidates[best];
+    if (int rc = ensure_table(B)) return rc;
+    if (cache_path) {
         char line[640];
+        auto mlups = [&](double ms) { return ms > 0.0 ? cells * steps_per_trial / (ms * 1e3) : 0.0; };
         std::snprintf(line, sizeof(line),
-                      "  {\"key\": \"%s\", \"class\": %d, \"V\": %d, \"rows\": %d, "
-                      "\"mlups\": %.1f, \"members\": %d}",
-                      key.c_str(), c, bv, 4, cells * steps_per_trial / (double(best) * 1e3),
-                      int(saved.size()));
-        timed.push_back(line);
-    }
-    for (lbm_lattice* L : B->members) {
-        const int c = width_class(L->w);
-        if (int rc = lbm_set_tile(L, choice[c][0], choice[c][1])) return rc;
-    }
-    if (cache_path && !timed.empty()) {
-        // rewrite: other keys kept, this key's classes (cached + new) written
-        for (int c = 0; c < 5; ++c) {
-            if (!have[c]) continue;
-            bool is_new = false;
-            for (const auto& t : timed)
-                if (t.find("\"class\": " + std::to_string(c) + ",") != std::string::npos) is_new = true;
-            if (is_new) continue;
-            char line[640];
-            std::snprintf(line, sizeof(line), "  {\"key\": \"%s\", \"class\": %d, \"V\": %d, \"rows\": %d}",
-                          key.c_str(), c, choice[c][0], choice[c][1]);
-            kept.push_back(line);
-        }
-        for (auto& t : timed) kept.push_back(t);
+                      "{\"key\": \"%s\", \"V\": %d, \"mlups_v2\": %.1f, \"mlups_v4\": %.1f, \"members\": %d}",
+                      key.c_str(), B->V, mlups(total_ms[0]), mlups(total_ms[1]), int(B->members.size()));
+        kept.push_back(line);
         FILE* fh = std::fopen(cache_path, "w");
         if (!fh) return bfail(LBM_ERR_INVALID_ARGUMENT, std::string("cannot write ") + cache_path);
         std::fprintf(fh, "{\"lbm_batch_autotune\": [\n");
         for (size_t k = 0; k < kept.size(); ++k) {
-            std::string s = kept[k];
-            while (!s.empty() && s.front() == ' ') s.erase(s.begin());
-            std::fprintf(fh, "  %s%s\n", s.c_str(), k + 1 < kept.size() ? "," : "");
+            std::string t = kept[k];
+            while (!t.empty() && t.front() == ' ') t.erase(t.begin());
+            std::fprintf(fh, "  %s%s\n", t.c_str(), k + 1 < kept.size() ? "," : "");
         }
         std::fprintf(fh, "]}\n");
         std::fclose(fh);

@@ -542,15 +542,21 @@ struct InteriorRows {
 
 // Interior warp tile (flag 0): every source cell is inside the lattice and
 // fluid, so a step is 9 vector loads, 6 shuffles and two edge scalars per
-// lane, the collision and 9 vector stores.
-template <class S, int V, int FRAME, bool FAST, bool SR = false>
+// lane, the collision and 9 vector stores.  With GEN_CT (a tile flagged 3 of
+// a lattice with link masks: solids nearby, no lattice edge in reach) the
+// same code applies the fixups of step_general from the tile's per-lane link
+// masks: bounce-back links take the cell's own opposite population, solid
+// cells swap (full-way) or keep their populations (half-way).
+template <class S, int V, int FRAME, bool FAST, bool SR = false, bool GEN_CT = false>
 __device__ __forceinline__ void step_interior(const StepArgs<typename Store<S>::CT>& a, int y,
-                                              int x0, int lane) {
+                                              int x0, int lane, int tile = 0) {
     using CT = typename Store<S>::CT;
     using ST = Store<S>;
     const S* __restrict__ src = static_cast<const S*>(a.src);
     const int64_t PL = a.plane;
     const InteriorRows rows(a, y, x0, V);
+    uint4 lk = make_uint4(0u, 0u, 0u, 0u);
+    if constexpr (GEN_CT) lk = __ldg(a.links + (int64_t(y) * a.ntiles + tile) * 32 + lane);
     S raw[9][V];
     S edge[9];
 #pragma unroll
@@ -583,10 +589,51 @@ __device__ __forceinline__ void step_interior(const StepArgs<typename Store<S>::
 #pragma unroll
         for (int k = 0; k < V; ++k) f[i][k] = v[k];
     }
+    constexpr uint32_t FULL = (1u << V) - 1u;
+    const uint32_t own_solid = GEN_CT ? (lk.x & FULL) : 0u;
+    const bool halfway = (a.flags & LBM_SOLID_HALFWAY) != 0;
+    if constexpr (GEN_CT) {
+        const uint32_t words[3] = {lk.x, lk.y, lk.z};
+#pragma unroll
+        for (int i = 1; i < 9; ++i) {
+            const uint32_t bnc = (words[i >> 2] >> (8 * (i & 3))) & FULL;
+            if (bnc) {
+                S own[V];
+                VecIO<S, V>::load(src + OPP(i) * PL + rows.r0 + x0, own);
+#pragma unroll
+                for (int k = 0; k < V; ++k)
+                    if ((bnc >> k) & 1u) f[i][k] = ST::dec_dom(own[k]);
+            }
+        }
+        if (own_solid && !halfway) {
+            // bounce_back (src/lbm.rs:741-751): solid nodes take swapped populations
+#pragma unroll
+            for (int k = 0; k < V; ++k) {
+                if ((own_solid >> k) & 1u) {
+                    CT t;
+                    t = f[1][k]; f[1][k] = f[3][k]; f[3][k] = t;
+                    t = f[2][k]; f[2][k] = f[4][k]; f[4][k] = t;
+                    t = f[5][k]; f[5][k] = f[7][k]; f[7][k] = t;
+                    t = f[6][k]; f[6][k] = f[8][k]; f[8][k] = t;
+                }
+            }
+        }
+    }
     collide_cells<S, V, FAST>(a.c, f);
     S enc[9][V];
 #pragma unroll
     for (int i = 0; i < 9; ++i) ST::enc_vec_dom(f[i], enc[i], SR ? 1 : 0);
+    if (GEN_CT && own_solid && halfway) {
+        // half-way mode: solid nodes keep their populations
+#pragma unroll
+        for (int i = 0; i < 9; ++i) {
+            S own[V];
+            VecIO<S, V>::load(src + i * PL + rows.r0 + x0, own);
+#pragma unroll
+            for (int k = 0; k < V; ++k)
+                if ((own_solid >> k) & 1u) enc[i][k] = own[k];
+        }
+    }
     store_cells<S, V, FAST>(a, y, x0, enc);
 }
 
@@ -1417,8 +1464,13 @@ constexpr int step_min_blocks() {
     if (sizeof(S) == 2) return V <= 4 ? LBM_STEP_MIN_BLOCKS_16 : LBM_STEP_MIN_BLOCKS_16_V8;
     return V <= 4 ? LBM_STEP_MIN_BLOCKS : 1;
 }
+#ifdef LBM_STEP_MAXNREG
+template <class S, int V, int FRAME, bool FAST, bool SR>
+__global__ void __maxnreg__(LBM_STEP_MAXNREG)
+#else
 template <class S, int V, int FRAME, bool FAST, bool SR>
 __global__ void __launch_bounds__(256, step_min_blocks<S, V>())
+#endif
 lbm_step_kernel(const StepArgs<typename Store<S>::CT> a) {
     const int rows = blockDim.y;
     const int gblocks = a.tflags != nullptr ? (a.ngtiles + rows - 1) / rows : 0;
@@ -1454,8 +1506,13 @@ lbm_step_kernel(const StepArgs<typename Store<S>::CT> a) {
         else if (flag == 3) step_interior_packed<S, V, FRAME, SR, true>(a, y, x0, threadIdx.x, tile);
         else step_interior_packed<S, V, FRAME, SR>(a, y, x0, threadIdx.x);
     } else {
-        if (flag & 1) return;                                              // 1, 3: owned by the list
+        // 1 and 3 are owned by the list, except 3 when link masks exist
+        if (flag == 1 || (flag == 3 && a.links == nullptr)) return;
         if (flag == 0) step_interior<S, V, FRAME, FAST, SR>(a, y, x0, threadIdx.x);
+        else if (flag == 3) {
+            if constexpr (LBM_LINKS_F32 && std::is_same<S, float>::value)
+                step_interior<S, V, FRAME, FAST, SR, true>(a, y, x0, threadIdx.x, tile);
+        }
         else step_interior_wrap<S, V, FRAME, FAST, SR>(a, y, x0, threadIdx.x);
     }
 }

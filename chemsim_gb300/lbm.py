@@ -279,6 +279,15 @@ class Batch:
     def set_stream(self, stream_ptr):
         check(self._lib.lbm_batch_set_stream(self._b, ctypes.c_void_p(stream_ptr or 0)))
 
+    def set_tile(self, cells_per_thread: int):
+        """The batch kernel's tile width, 2 or 4 cells per thread."""
+        check(self._lib.lbm_batch_set_tile(self._b, int(cells_per_thread)))
+
+    def tile(self) -> int:
+        v = ctypes.c_int32()
+        check(self._lib.lbm_batch_tile(self._b, ctypes.byref(v)))
+        return v.value
+
     def autotune(self, cache_path: str | None = None, steps_per_trial: int = 0):
         path = cache_path.encode() if cache_path else None
         check(self._lib.lbm_batch_autotune(self._b, path, int(steps_per_trial)))

@@ -252,19 +252,27 @@ int lbm_batch_destroy(lbm_batch* batch);
 int lbm_batch_size(lbm_batch* batch, int* n);
 int lbm_batch_lattice(lbm_batch* batch, int index, lbm_lattice** out);
 
-/* Advances every member nsteps steps (the per-step launches replayed from a
- * CUDA graph); each member's time and step count advance as with lbm_step.
- * Asynchronous on the batch's stream.                                      */
+/* Advances every member nsteps steps: one kernel launch per step covers
+ * every member (runs of 16 steps replay a captured CUDA graph); each
+ * member's time and step count advance as with lbm_step.  Asynchronous on
+ * the batch's stream.                                                      */
 int lbm_batch_step(lbm_batch* batch, int nsteps);
 int lbm_batch_synchronize(lbm_batch* batch);
 int lbm_batch_set_stream(lbm_batch* batch, void* stream);
 
-/* Picks the warp-tile width (cells per thread) for each width class of the
- * members (<= 96, <= 192, <= 384, <= 768, wider) by timing the candidates on
- * the class's own members, whose state (populations, time, step count) is
- * saved before and restored after; applies it and caches the choice in the
- * JSON file cache_path (NULL: no cache).  A cached entry for this GPU and
- * mode is reused without timing.  steps_per_trial <= 0 selects 24.         */
+/* The batch's warp-tile width: 2 or 4 cells per thread (default 4), one
+ * batch kernel each.  Batch steps run every member at this width; a member
+ * set to another one with lbm_set_tile is set back at the next batch step.
+ * Results do not depend on it.                                             */
+int lbm_batch_set_tile(lbm_batch* batch, int cells_per_thread);
+int lbm_batch_tile(lbm_batch* batch, int* cells_per_thread);
+
+/* Picks the batch's tile width by timing both candidates on the members,
+ * one width class (<= 96, <= 192, <= 384, <= 768, wider) at a time, whose
+ * state (populations, time, step count) is saved before and restored after;
+ * applies it and caches the choice in the JSON file cache_path (NULL: no
+ * cache).  A cached entry for this GPU and mode is reused without timing.
+ * steps_per_trial <= 0 selects 24.                                         */
 int lbm_batch_autotune(lbm_batch* batch, const char* cache_path, int steps_per_trial);
 
 /* ---- checkpoint / resume --------------------------------------------------

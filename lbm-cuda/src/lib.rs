@@ -119,6 +119,8 @@ pub mod ffi {
         pub fn lbm_batch_step(b: *mut LbmBatch, nsteps: c_int) -> c_int;
         pub fn lbm_batch_synchronize(b: *mut LbmBatch) -> c_int;
         pub fn lbm_batch_set_stream(b: *mut LbmBatch, stream: *mut c_void) -> c_int;
+        pub fn lbm_batch_set_tile(b: *mut LbmBatch, cells_per_thread: c_int) -> c_int;
+        pub fn lbm_batch_tile(b: *mut LbmBatch, cells_per_thread: *mut c_int) -> c_int;
         pub fn lbm_batch_autotune(b: *mut LbmBatch, cache_path: *const c_char, steps_per_trial: c_int) -> c_int;
         // learned coarse-grid correction
         pub fn lbm_cnn_create(h: c_int, w: c_int, max_batch: c_int, seed: u64, out: *mut *mut LbmCnn) -> c_int;
@@ -363,8 +365,19 @@ impl CudaBatch {
         ok(unsafe { lbm_batch_step(self.raw, n as c_int) })
     }
 
-    /// Times each size class's tile widths on the members and caches the
-    /// choice in the JSON file at `cache`.
+    /// The batch kernel's tile width: 2 or 4 cells per thread.
+    pub fn set_tile(&mut self, cells_per_thread: usize) {
+        ok(unsafe { lbm_batch_set_tile(self.raw, cells_per_thread as c_int) })
+    }
+
+    pub fn tile(&self) -> usize {
+        let mut v: c_int = 0;
+        ok(unsafe { lbm_batch_tile(self.raw, &mut v) });
+        v as usize
+    }
+
+    /// Times both tile widths on the members and caches the choice in the
+    /// JSON file at `cache`.
     pub fn autotune(&mut self, cache: &Path) {
         let p = c_path(cache);
         ok(unsafe { lbm_batch_autotune(self.raw, p.as_ptr(), 0) })

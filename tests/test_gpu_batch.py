@@ -102,8 +102,9 @@ def test_autotune_writes_and_reuses_cache(gpu, tmp_path):
             assert m.time() == (0.0, 0)
         doc = json.loads(cache.read_text())
         entries = doc["lbm_batch_autotune"]
-        assert entries and all(e["V"] in (2, 4) and e["rows"] in (1, 2, 4, 8) for e in entries)
-        classes = {e["class"] for e in entries}
+        assert len(entries) == 1 and entries[0]["V"] in (2, 4)
+        assert entries[0]["mlups_v2"] > 0 and entries[0]["mlups_v4"] > 0
+        chosen = entries[0]["V"]
         first = cache.read_text()
         b.autotune(str(cache))            # cached: nothing timed, file unchanged
         assert cache.read_text() == first
@@ -111,7 +112,29 @@ def test_autotune_writes_and_reuses_cache(gpu, tmp_path):
         for m, sp in zip(b.members, specs):
             ref, _ = _single(sp, FRAME_XY | FAST, 21)
             assert np.array_equal(m.get_populations(), ref), sp.name
-    assert classes
+    # a new batch of the same mode takes the cached width without timing
+    with Batch(specs[:2], FRAME_XY | FAST) as b:
+        b.autotune(str(cache))
+        assert cache.read_text() == first
+        assert b.tile() == chosen
+
+
+@pytest.mark.parametrize("tile", [2, 4])
+def test_batch_tile_widths_equal_single_lattices(gpu, tile):
+    """Both batch kernels (2 and 4 cells per thread), with members whose own
+    tile width differs from the batch's (reset to it at the next step)."""
+    specs = _specs(8, seed=13)
+    with Batch(specs, FRAME_XY | FAST) as b:
+        _init(b, specs)
+        b.set_tile(tile)
+        b.members[1].set_tile(8 if tile == 4 else 4, 2)
+        b.step(19)
+        for m, sp in zip(b.members, specs):
+            ref, _ = _single(sp, FRAME_XY | FAST, 19)
+            assert np.array_equal(m.get_populations(), ref), sp.name
+        assert b.tile() == tile
+    with Batch(specs[:1], FRAME_XY | FAST) as b, pytest.raises(lbm.LBMError):
+        b.set_tile(8)
 
 
 def test_batch_rejects_bad_flags(gpu):
