@@ -102,6 +102,8 @@ def parse_args():
     p.add_argument("--no-batch", action="store_true", help="skip the 512-lattice batch")
     p.add_argument("--batch-steps", type=int, default=2000)
     p.add_argument("--batch-lattices", type=int, default=512)
+    p.add_argument("--batch-tile", type=int, default=0, choices=(0, 2, 4),
+                   help="batch tile width in cells per thread (0: autotuned)")
     p.add_argument("--no-large", action="store_true",
                    help="skip the 16384^2 f16 / 8192^2 f32 comparison")
     p.add_argument("--large-steps", type=int, default=500)
@@ -528,10 +530,14 @@ def run_batch(args, torch):
     if os.path.exists(cache):
         os.unlink(cache)
     t0 = time.perf_counter()
-    b.autotune(cache)
+    if args.batch_tile:
+        b.set_tile(args.batch_tile)
+        tuned = None
+    else:
+        b.autotune(cache)
+        with open(cache) as fh:
+            tuned = json.load(fh)["lbm_batch_autotune"][-1]
     tune_s = time.perf_counter() - t0
-    with open(cache) as fh:
-        tuned = json.load(fh)["lbm_batch_autotune"][-1]
     b.step(args.warmup)
     b.synchronize()
     start = torch.cuda.Event(enable_timing=True)
@@ -552,7 +558,7 @@ def run_batch(args, torch):
             "achieved_gbs": round(gbs, 1), "frac": round(gbs / peak, 4),
             "ms_per_step": round(secs / args.batch_steps * 1e3, 4), "autotune_s": round(tune_s, 2),
             "tile_cells_per_thread": tile,
-            "autotune_mlups": {"2": tuned["mlups_v2"], "4": tuned["mlups_v4"]},
+            "autotune_mlups": {"2": tuned["mlups_v2"], "4": tuned["mlups_v4"]} if tuned else None,
             "launches_per_step": 1,
             "stable": all(not h["unstable"] for h in health)}
 

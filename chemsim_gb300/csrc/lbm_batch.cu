@@ -4,7 +4,7 @@
 // single-lattice entry point works on a member) and advances all of them by
 // one launch per time step.  The launch covers a list of work items, one per
 // warp: (member, row, warp tile) of every member, general items first, then
-// each member in blocks of 8 rows of one tile column, so the 8 warps of a CTA
+// each member in blocks of 4 rows of one tile column, so the 4 warps of a CTA
 // share the rows they pull from.  Each warp runs the same interior / general /
 // link-mask step code as a single lattice, so a member's results do not depend
 // on whether it was stepped alone or in a batch.  Runs of steps replay a
@@ -46,7 +46,10 @@ struct lbm_batch {
 
 namespace {
 
-constexpr int kTaskWarps = 8;
+#ifndef LBM_BATCH_WARPS
+#define LBM_BATCH_WARPS 4
+#endif
+constexpr int kTaskWarps = LBM_BATCH_WARPS;
 constexpr int kBatchGraphSteps = 16;
 constexpr int kDefaultV = 4;
 
@@ -55,6 +58,10 @@ enum : uint32_t { kGeneral = 0, kWrap = 1, kInterior = 2, kLinks = 3 };
 
 #ifndef LBM_BATCH_PREFETCH
 #define LBM_BATCH_PREFETCH 1
+#endif
+// Prefetch distance in percent of the resident warps (one wave: 100).
+#ifndef LBM_BATCH_PF_PCT
+#define LBM_BATCH_PF_PCT 100
 #endif
 
 // L2 prefetch of the rows item q pulls, one plane a lane (the range is
@@ -78,13 +85,11 @@ __device__ __forceinline__ void prefetch_item(const lbm_batch_member_dev* __rest
 // One warp = one work item: the kind dispatch is warp-uniform.  After its own
 // item the warp prefetches into L2 the rows of the item about one wave of
 // resident warps ahead (after, not before: the prefetch first reads that
-// item and its member's arguments).  Registers: V = 4 at 3 CTAs of 8 warps
-// per SM (80 a thread), V = 2 at 4 (64); the general path spills a little at
-// both, the interior paths fit.
+// item and its member's arguments).
 template <int V, int FRAME, bool FAST>
-__global__ void __launch_bounds__(256, V == 2 ? 4 : 3)
-lbm_batch_kernel(const lbm_batch_member_dev* __restrict__ members, const uint2* __restrict__ items,
-                 int nitems, int parity, int pf) {
+__device__ __forceinline__ void batch_item(const lbm_batch_member_dev* __restrict__ members,
+                                           const uint2* __restrict__ items, int nitems, int parity,
+                                           int pf) {
     const int lane = threadIdx.x;
     const int it = blockIdx.x * blockDim.y + threadIdx.y;
     if (it >= nitems) return;
@@ -101,15 +106,36 @@ lbm_batch_kernel(const lbm_batch_member_dev* __restrict__ members, const uint2* 
     prefetch_item<V, FRAME>(members, items, nitems, it + pf, parity, lane);
 }
 
+// Registers, CTAs of 4 warps: 4 cells per thread capped at 96 (5 CTAs per
+// SM), 2 cells at 64 (8 CTAs); the general path spills a little at both.
+// 512-member mix, one GB300, fraction of the copy bandwidth at 4 cells per
+// thread: CTAs of 8 warps at 80 registers 0.765, of 4 warps at 80 0.775, of
+// 4 warps at 96 0.784.
+#ifndef LBM_BATCH_V4_MAXNREG
+#define LBM_BATCH_V4_MAXNREG 96
+#endif
+template <int FRAME, bool FAST>
+__global__ void __maxnreg__(LBM_BATCH_V4_MAXNREG)
+lbm_batch_kernel_v4(const lbm_batch_member_dev* __restrict__ members, const uint2* __restrict__ items,
+                    int nitems, int parity, int pf) {
+    batch_item<4, FRAME, FAST>(members, items, nitems, parity, pf);
+}
+template <int FRAME, bool FAST>
+__global__ void __launch_bounds__(256, 4)
+lbm_batch_kernel_v2(const lbm_batch_member_dev* __restrict__ members, const uint2* __restrict__ items,
+                    int nitems, int parity, int pf) {
+    batch_item<2, FRAME, FAST>(members, items, nitems, parity, pf);
+}
+
 using BatchKernel = void (*)(const lbm_batch_member_dev*, const uint2*, int, int, int);
 
 BatchKernel pick_kernel(int V, int frame, int fast) {
     if (V == 2) {
-        if (frame) return fast ? lbm_batch_kernel<2, 1, true> : lbm_batch_kernel<2, 1, false>;
-        return fast ? lbm_batch_kernel<2, 0, true> : lbm_batch_kernel<2, 0, false>;
+        if (frame) return fast ? lbm_batch_kernel_v2<1, true> : lbm_batch_kernel_v2<1, false>;
+        return fast ? lbm_batch_kernel_v2<0, true> : lbm_batch_kernel_v2<0, false>;
     }
-    if (frame) return fast ? lbm_batch_kernel<4, 1, true> : lbm_batch_kernel<4, 1, false>;
-    return fast ? lbm_batch_kernel<4, 0, true> : lbm_batch_kernel<4, 0, false>;
+    if (frame) return fast ? lbm_batch_kernel_v4<1, true> : lbm_batch_kernel_v4<1, false>;
+    return fast ? lbm_batch_kernel_v4<0, true> : lbm_batch_kernel_v4<0, false>;
 }
 
 int bfail(int code, const std::string& msg) { return lattice_fail(code, msg); }
@@ -200,7 +226,7 @@ int ensure_table(lbm_batch* B) {
 cudaError_t launch(lbm_batch* B, int parity) {
     if (B->ntasks == 0) return cudaSuccess;
     const int grid = (B->ntasks + kTaskWarps - 1) / kTaskWarps;
-    const int pf = std::max(1, B->resident[B->V == 4]);
+    const int pf = std::max(1, int(int64_t(B->resident[B->V == 4]) * LBM_BATCH_PF_PCT / 100));
     pick_kernel(B->V, B->frame, B->fast)<<<grid, dim3(32, kTaskWarps), 0, B->stream>>>(
         B->d_members, B->d_tasks, B->ntasks, parity, pf);
     return cudaGetLastError();

@@ -1464,14 +1464,8 @@ constexpr int step_min_blocks() {
     if (sizeof(S) == 2) return V <= 4 ? LBM_STEP_MIN_BLOCKS_16 : LBM_STEP_MIN_BLOCKS_16_V8;
     return V <= 4 ? LBM_STEP_MIN_BLOCKS : 1;
 }
-#ifdef LBM_STEP_MAXNREG
 template <class S, int V, int FRAME, bool FAST, bool SR>
-__global__ void __maxnreg__(LBM_STEP_MAXNREG)
-#else
-template <class S, int V, int FRAME, bool FAST, bool SR>
-__global__ void __launch_bounds__(256, step_min_blocks<S, V>())
-#endif
-lbm_step_kernel(const StepArgs<typename Store<S>::CT> a) {
+__device__ __forceinline__ void step_block(const StepArgs<typename Store<S>::CT>& a) {
     const int rows = blockDim.y;
     const int gblocks = a.tflags != nullptr ? (a.ngtiles + rows - 1) / rows : 0;
     const int b = blockIdx.x;
@@ -1517,6 +1511,28 @@ lbm_step_kernel(const StepArgs<typename Store<S>::CT> a) {
     }
 }
 
+// The step kernels.  16-bit storage at 8 cells per thread is capped at 96
+// registers (5 blocks of 4 warps per SM, ~300 B of spills in the general
+// paths) instead of 128 (4 blocks): 4096^2 obstacle channel, stochastic
+// rounding, one GB300: 156.4k -> 160.2k MLUPS (88 registers 156.2k, 104
+// registers 149.8k).  Every other kernel is sized by step_min_blocks.
+#ifndef LBM_STEP16_V8_MAXNREG
+#define LBM_STEP16_V8_MAXNREG 96
+#endif
+template <class S, int V, int FRAME, bool FAST, bool SR>
+__global__ void __launch_bounds__(256, step_min_blocks<S, V>())
+lbm_step_kernel(const StepArgs<typename Store<S>::CT> a) {
+    step_block<S, V, FRAME, FAST, SR>(a);
+}
+template <class S, int V, int FRAME, bool FAST, bool SR>
+__global__ void __maxnreg__(LBM_STEP16_V8_MAXNREG)
+lbm_step_kernel_capped(const StepArgs<typename Store<S>::CT> a) {
+    step_block<S, V, FRAME, FAST, SR>(a);
+}
+
+template <class S, int V>
+constexpr bool step_capped() { return sizeof(S) == 2 && V == 8; }
+
 // Prefetch distance, in percent of the rows the resident blocks cover (the
 // wavefront's depth): far enough that the prefetched rows arrive before
 // their warps start, near enough that they are still in L2.
@@ -1543,9 +1559,14 @@ void launch_step_tv(const StepArgs<typename Store<S>::CT>& a, int rows, cudaStre
                 return out;
             for (int r = 1; r <= 8; ++r) {
                 int occ = 0;
-                if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                        &occ, lbm_step_kernel<S, V, FRAME, FAST, SR>, 32 * r, 0) == cudaSuccess)
-                    out[r] = occ * sms;
+                cudaError_t e;
+                if constexpr (step_capped<S, V>())
+                    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                        &occ, lbm_step_kernel_capped<S, V, FRAME, FAST, SR>, 32 * r, 0);
+                else
+                    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                        &occ, lbm_step_kernel<S, V, FRAME, FAST, SR>, 32 * r, 0);
+                if (e == cudaSuccess) out[r] = occ * sms;
             }
             (void)cudaGetLastError();
             return out;
@@ -1553,7 +1574,11 @@ void launch_step_tv(const StepArgs<typename Store<S>::CT>& a, int rows, cudaStre
         const int64_t wave_rows = int64_t(blocks_per_gpu[rows]) * rows / ntiles;
         b.pf_rows = int(wave_rows * LBM_PREFETCH_PCT / 100);
     }
-    lbm_step_kernel<S, V, FRAME, FAST, SR><<<gblocks + ntiles * rowblocks, dim3(32, rows), 0, stream>>>(b);
+    const int grid = gblocks + ntiles * rowblocks;
+    if constexpr (step_capped<S, V>())
+        lbm_step_kernel_capped<S, V, FRAME, FAST, SR><<<grid, dim3(32, rows), 0, stream>>>(b);
+    else
+        lbm_step_kernel<S, V, FRAME, FAST, SR><<<grid, dim3(32, rows), 0, stream>>>(b);
 }
 
 // One step: the interior kernel plus the general kernel over the flagged

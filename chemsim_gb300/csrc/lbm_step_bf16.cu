@@ -1,7 +1,4 @@
 // lbm_step_bf16.cu — fused-step launches for bfloat16 deviation storage.
-#if defined(LBM_STEP16_MAXNREG) && !defined(LBM_STEP_MAXNREG)
-#define LBM_STEP_MAXNREG LBM_STEP16_MAXNREG
-#endif
 #include "lbm_step.cuh"
 
 namespace lbmk {
