@@ -61,7 +61,7 @@ enum : uint32_t { kGeneral = 0, kWrap = 1, kInterior = 2, kLinks = 3 };
 #endif
 // Prefetch distance in percent of the resident warps (one wave: 100).
 #ifndef LBM_BATCH_PF_PCT
-#define LBM_BATCH_PF_PCT 100
+#define LBM_BATCH_PF_PCT 130
 #endif
 
 // L2 prefetch of the rows item q pulls, one plane a lane (the range is
