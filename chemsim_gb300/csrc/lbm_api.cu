@@ -474,6 +474,7 @@ int lattice_readback_stream(lbm_lattice* L) {
     LBM_CUDA(cudaStreamCreateWithFlags(&L->rb_stream, cudaStreamNonBlocking));
     LBM_CUDA(cudaEventCreateWithFlags(&L->rb_staged, cudaEventDisableTiming));
     LBM_CUDA(cudaEventCreateWithFlags(&L->rb_landed, cudaEventDisableTiming));
+    for (auto& e : L->rb_done) LBM_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     return LBM_OK;
 }
 
@@ -643,10 +644,11 @@ int lbm_destroy(lbm_lattice* L) {
         if (L->health) cudaFree(L->health);
         if (L->render) cudaFree(L->render);
         if (L->rb_stream) cudaStreamSynchronize(L->rb_stream);
-        if (L->rb) cudaFree(L->rb);
+        for (auto& b : L->rb) if (b) cudaFree(b);
         if (L->rb_stream) cudaStreamDestroy(L->rb_stream);
         if (L->rb_staged) cudaEventDestroy(L->rb_staged);
         if (L->rb_landed) cudaEventDestroy(L->rb_landed);
+        for (auto& e : L->rb_done) if (e) cudaEventDestroy(e);
         if (L->tflags) cudaFree(L->tflags);
         if (L->gtiles) cudaFree(L->gtiles);
         if (L->links) cudaFree(L->links);
@@ -813,26 +815,35 @@ int lbm_read_moments_async(lbm_lattice* L, float* rho, float* ux, float* uy) {
     DeviceGuard g(L->dev);
     const size_t plane = size_t(L->w) * L->h;
     if (int rc = lattice_readback_stream(L)) return rc;
-    if (!L->rb) {
+    if (!L->rb[0]) {
+        // both staging areas at once, so no later call allocates
         if (L->rb_pending) LBM_CUDA(cudaEventSynchronize(L->rb_landed));
-        LBM_CUDA(cudaMalloc(reinterpret_cast<void**>(&L->rb), 3 * plane * sizeof(float)));
+        for (auto& b : L->rb) LBM_CUDA(cudaMalloc(reinterpret_cast<void**>(&b), 3 * plane * sizeof(float)));
     }
     if (!L->mom_valid) {
         if (int rc = LBM_DISPATCH(L, moments_t, L)) return rc;
         L->mom_valid = true;
     }
-    // the staging area is reused: its previous host copy must have finished
-    if (L->rb_pending) LBM_CUDA(cudaStreamWaitEvent(L->stream, L->rb_landed, 0));
+    // Two staging areas in turn: this one's previous host copy must have
+    // finished; the other one's may still run while this one is staged and
+    // the next steps run.
+    const int i = L->rb_next;
+    L->rb_next ^= 1;
+    float* rb = L->rb[i];
+    if (L->rb_used[i]) LBM_CUDA(cudaStreamWaitEvent(L->stream, L->rb_done[i], 0));
     for (int m = 0; m < 3; ++m)
-        LBM_CUDA(cudaMemcpy2DAsync(L->rb + m * plane, size_t(L->w) * 4, L->mom[m],
+        LBM_CUDA(cudaMemcpy2DAsync(rb + m * plane, size_t(L->w) * 4, L->mom[m],
                                    size_t(L->pitch) * 4, size_t(L->w) * 4, L->h,
                                    cudaMemcpyDeviceToDevice, L->stream));
     LBM_CUDA(cudaEventRecord(L->rb_staged, L->stream));
     LBM_CUDA(cudaStreamWaitEvent(L->rb_stream, L->rb_staged, 0));
     float* dst[3] = {rho, ux, uy};
     for (int m = 0; m < 3; ++m)
-        LBM_CUDA(cudaMemcpyAsync(dst[m], L->rb + m * plane, plane * sizeof(float),
+        LBM_CUDA(cudaMemcpyAsync(dst[m], rb + m * plane, plane * sizeof(float),
                                  cudaMemcpyDeviceToHost, L->rb_stream));
+    LBM_CUDA(cudaEventRecord(L->rb_done[i], L->rb_stream));
+    L->rb_used[i] = true;
+    // the copy stream is in order: the latest landing covers every earlier one
     LBM_CUDA(cudaEventRecord(L->rb_landed, L->rb_stream));
     L->rb_pending = true;
     return LBM_OK;

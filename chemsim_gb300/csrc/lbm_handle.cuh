@@ -22,9 +22,12 @@ struct lbm_lattice {
     lbmk::HealthPartial* health = nullptr;  // kHealthBlocks partials + 1 result
     void* render = nullptr;               // colour-map scratch (stats, host-bound image)
     size_t render_bytes = 0;
-    float* rb = nullptr;                  // staged moments of an asynchronous readback
-    cudaStream_t rb_stream = nullptr;     // its device-to-host copies
-    cudaEvent_t rb_staged = nullptr, rb_landed = nullptr;
+    float* rb[2] = {nullptr, nullptr};    // staged moments of asynchronous readbacks, used in turn
+    cudaEvent_t rb_done[2] = {nullptr, nullptr};  // the host copy out of rb[i] has finished
+    bool rb_used[2] = {false, false};     // rb_done[i] has been recorded
+    int rb_next = 0;                      // staging area of the next readback
+    cudaStream_t rb_stream = nullptr;     // their device-to-host copies
+    cudaEvent_t rb_staged = nullptr, rb_landed = nullptr;   // rb_landed: the latest readback landed
     bool rb_pending = false;
     uint8_t* tflags = nullptr;            // h x ceil(w / 32) bytes
     int ntiles = 0;

@@ -165,8 +165,9 @@ int lbm_read_moments(lbm_lattice* lat, float* rho, float* ux, float* uy,
  * device-to-device copy), then copied to the host on a second stream, so
  * following steps run while that copy is in flight.  The host buffers
  * (pinned, for the copy to overlap) must stay valid and unread until
- * lbm_readback_wait returns.  One readback is in flight at a time: the next
- * one's staging waits on the device for the previous host copy.            */
+ * lbm_readback_wait returns.  Two device staging areas are used in turn, so
+ * a readback is staged while the previous one's host copy is in flight; the
+ * host copies run one after another on the second stream.                 */
 int lbm_read_moments_async(lbm_lattice* lat, float* rho, float* ux, float* uy);
 /* nsteps time steps whose last one writes rho/u straight into rho, ux, uy:
  * w*h floats each, row-major y*w+x, in memory the GPU addresses (device or
@@ -226,8 +227,8 @@ int lbm_set_tile(lbm_lattice* lat, int cells_per_thread, int rows_per_block);
 
 /* ---- batches of independent lattices ----------------------------------- */
 /* No reference counterpart: many lattices of uneven sizes and relaxation
- * times advanced together, each time step a few launches (one per non-empty
- * (tile width, path) work list) over warp work items of all members.       */
+ * times advanced together, each time step one kernel launch over the warp
+ * work items (row, warp tile) of all members.                             */
 
 typedef struct lbm_batch lbm_batch;
 
@@ -303,8 +304,8 @@ int lbm_load(lbm_lattice* lat, const char* path);
 #define LBM_RENDER_MOMENTUM 3
 int lbm_render(lbm_lattice* lat, int mode, int geometry_overlay, uint8_t* rgba, int on_device);
 /* The same frame copied to host memory without waiting, like
- * lbm_read_moments_async (and sharing its one-in-flight readback): rgba
- * (pinned, for overlap) holds the frame once lbm_readback_wait returns.    */
+ * lbm_read_moments_async (its staging waits for every readback in flight):
+ * rgba (pinned, for overlap) holds the frame once lbm_readback_wait returns. */
 int lbm_render_async(lbm_lattice* lat, int mode, int geometry_overlay, uint8_t* rgba);
 
 /* ---- learned coarse-grid correction --------------------------------------
