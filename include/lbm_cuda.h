@@ -210,11 +210,11 @@ int lbm_device_populations(lbm_lattice* lat, void** base, int64_t* plane_stride,
  * (16384 x 16384); larger lattices return LBM_ERR_INVALID_ARGUMENT.  The
  * first call in each CUDA context (a device's primary context, the new one
  * that follows cudaDeviceReset, or a context the caller made current)
- * resolves the array's device address in that context (make that first call
- * before any stream capture).  Calls share the array, so calls
- * that overlap on the GPU race; every call overwrites all of the scratch it
- * reads, so nothing needs clearing between calls.  Synchronises `stream`;
- * out->steps is 0.                                                          */
+ * resolves the array's device address in that context.  Not callable while
+ * `stream` (or the legacy stream) is being captured: it copies its result to
+ * the host and synchronises `stream`.  Calls share the array, so calls that
+ * overlap on the GPU race; every call overwrites all of the scratch it
+ * reads, so nothing needs clearing between calls.  out->steps is 0.        */
 int lbm_check_device_noalloc(const void* populations, int precision, int w, int h,
                              int row_pitch, int64_t plane_stride, float delta_x,
                              float delta_t, void* stream, lbm_health* out);

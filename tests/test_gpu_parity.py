@@ -544,6 +544,35 @@ def test_async_moment_readback_is_a_snapshot(gpu):
         assert np.array_equal(pin[1], b.moments()[1])
 
 
+def test_async_readbacks_in_flight_back_to_back(gpu):
+    """Several lbm_read_moments_async calls without waiting in between (the
+    two device staging areas are used in turn, so a readback is staged while
+    the previous host copy runs): each host buffer set holds the fields of
+    the step it was called at."""
+    import torch
+    spec = channel_spec(512, n_obstacles=4, r_lo=6, r_hi=12, force=1e-5, seed=6, h=256)
+    flags = spec.flags | FAST
+
+    def lattice():
+        lat = Lattice(spec.w, spec.h, spec.tau, F32, flags)
+        lat.set_force(*spec.force)
+        lat.set_geometry(spec.solid)
+        lat.init_equilibrium(spec.rho, spec.ux, spec.uy)
+        return lat
+
+    sets = [[torch.empty((spec.h, spec.w), dtype=torch.float32).pin_memory().numpy() for _ in range(3)]
+            for _ in range(5)]
+    with lattice() as a, lattice() as b:
+        for k, out in enumerate(sets):
+            a.step(k + 1)
+            a.read_moments_async(*out)
+        a.readback_wait()
+        for k, out in enumerate(sets):
+            b.step(k + 1)
+            rho, ux, uy = b.moments()
+            assert np.array_equal(out[0], rho) and np.array_equal(out[1], ux) and np.array_equal(out[2], uy), k
+
+
 # -- interior paths against the general path ---------------------------------
 
 def _raw_planes(lat, path):
