@@ -22,15 +22,28 @@
 using namespace lbmk;
 
 struct lbm_batch_member_dev {
-    StepArgs<float> a[2];   // from the member's buffer at build time (0) or the other (1)
+    StepArgs<float> a;      // the member's step arguments at build time (both parities
+                            // share everything but src / dst, which the items carry)
 };
+
+// One warp's work item, 32 bytes: everything a warp needs to issue its
+// population loads, so no dependent read precedes them.
+struct BatchItem {
+    const float* buf0;      // the member's buffer that is the source at parity 0
+    const float* buf1;      // the other buffer
+    uint32_t member_kind;   // member index | kind << 24
+    uint32_t row_tile;      // row << 12 | warp tile
+    uint32_t w_pitch;       // w | (row pitch / 32) << 18
+    uint32_t h;
+};
+static_assert(sizeof(BatchItem) == 32, "32-byte items");
 
 struct lbm_batch {
     std::vector<lbm_lattice*> members;
     std::vector<uint64_t> built_version;
     std::vector<int> built_cur;
     lbm_batch_member_dev* d_members = nullptr;
-    uint2* d_tasks = nullptr;         // work items (member | kind << 24, row << 12 | tile)
+    BatchItem* d_tasks = nullptr;     // work items
     int ntasks = 0;
     size_t tasks_cap = 0;
     int par = 0;                      // steps since the table was built, mod 2
@@ -64,46 +77,76 @@ enum : uint32_t { kGeneral = 0, kWrap = 1, kInterior = 2, kLinks = 3 };
 #define LBM_BATCH_PF_PCT 130
 #endif
 
+// A batch item's step arguments in the shape the step code reads: the
+// addressing fields come from the item; the member's other arguments
+// (collision constants, flags, mask, link masks) are read from the member
+// table where a path uses them, after the population loads are issued.
+// Moment outputs and the single-lattice prefetch are compiled out.
+struct BatchView {
+    const void* src;
+    void* dst;
+    int64_t plane;
+    int pitch, w, h;
+    const Consts<float>& c;
+    const int& flags;
+    const uint8_t* const& solid;
+    const int& mpitch;
+    const int& ntiles;
+    const uint4* const& links;
+    static constexpr float* mom_rho = nullptr;
+    static constexpr float* mom_ux = nullptr;
+    static constexpr float* mom_uy = nullptr;
+    static constexpr int mom_pitch = 0;
+    static constexpr int pf_rows = 0;
+    __device__ __forceinline__ BatchView(const BatchItem& it, const StepArgs<float>& m, int parity)
+        : src(parity ? it.buf1 : it.buf0),
+          dst(const_cast<float*>(parity ? it.buf0 : it.buf1)),
+          plane(int64_t((it.w_pitch >> 18) * 32u) * it.h),
+          pitch(int((it.w_pitch >> 18) * 32u)),
+          w(int(it.w_pitch & 0x3ffffu)),
+          h(int(it.h)),
+          c(m.c), flags(m.flags), solid(m.solid), mpitch(m.mpitch), ntiles(m.ntiles), links(m.links) {}
+};
+
 // L2 prefetch of the rows item q pulls, one plane a lane (the range is
 // clipped to the row's pitch, so it stays inside the member's buffer).
 template <int V, int FRAME>
-__device__ __forceinline__ void prefetch_item(const lbm_batch_member_dev* __restrict__ members,
-                                              const uint2* __restrict__ items, int nitems, int q,
+__device__ __forceinline__ void prefetch_item(const BatchItem* __restrict__ items, int nitems, int q,
                                               int parity, int lane) {
     if (!LBM_BATCH_PREFETCH || lane >= 9 || q >= nitems) return;
-    const uint2 next = items[q];
-    const StepArgs<float>& an = members[next.x & 0xffffffu].a[parity];
-    const int ys = int(next.y >> 12) - DROW(FRAME, lane);
-    const int x0 = int(next.y & 4095u) * 32 * V;
-    if (ys >= 0 && ys < an.h) {
-        const int n = min(32 * V, an.pitch - x0);
-        const float* p = static_cast<const float*>(an.src) + lane * an.plane + int64_t(ys) * an.pitch + x0;
+    const BatchItem next = items[q];
+    const int h = int(next.h), pitch = int((next.w_pitch >> 18) * 32u);
+    const int ys = int(next.row_tile >> 12) - DROW(FRAME, lane);
+    const int x0 = int(next.row_tile & 4095u) * 32 * V;
+    if (ys >= 0 && ys < h) {
+        const int n = min(32 * V, pitch - x0);
+        const float* p = (parity ? next.buf1 : next.buf0) + lane * (int64_t(pitch) * h) +
+                         int64_t(ys) * pitch + x0;
         asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" :: "l"(p), "r"(n * 4) : "memory");
     }
 }
 
 // One warp = one work item: the kind dispatch is warp-uniform.  After its own
-// item the warp prefetches into L2 the rows of the item about one wave of
-// resident warps ahead (after, not before: the prefetch first reads that
-// item and its member's arguments).
+// item the warp prefetches into L2 the rows of the item about 1.3 waves of
+// resident warps ahead.
 template <int V, int FRAME, bool FAST>
 __device__ __forceinline__ void batch_item(const lbm_batch_member_dev* __restrict__ members,
-                                           const uint2* __restrict__ items, int nitems, int parity,
+                                           const BatchItem* __restrict__ items, int nitems, int parity,
                                            int pf) {
     const int lane = threadIdx.x;
     const int it = blockIdx.x * blockDim.y + threadIdx.y;
     if (it >= nitems) return;
-    const uint2 item = items[it];
-    const StepArgs<float>& a = members[item.x & 0xffffffu].a[parity];
-    const int y = int(item.y >> 12), tile = int(item.y & 4095u);
+    const BatchItem item = items[it];
+    const BatchView a(item, members[item.member_kind & 0xffffffu].a, parity);
+    const int y = int(item.row_tile >> 12), tile = int(item.row_tile & 4095u);
     const int x0 = (tile * 32 + lane) * V;
-    switch (item.x >> 24) {      // warp-uniform
+    switch (item.member_kind >> 24) {      // warp-uniform
         case kGeneral: step_general<float, V, FRAME, FAST>(a, y, tile, lane); break;
         case kWrap: step_interior_wrap<float, V, FRAME, FAST>(a, y, x0, lane); break;
         case kInterior: step_interior<float, V, FRAME, FAST>(a, y, x0, lane); break;
         default: step_interior<float, V, FRAME, FAST, false, true>(a, y, x0, lane, tile); break;
     }
-    prefetch_item<V, FRAME>(members, items, nitems, it + pf, parity, lane);
+    prefetch_item<V, FRAME>(items, nitems, it + pf, parity, lane);
 }
 
 // Registers, CTAs of 4 warps: 4 cells per thread capped at 96 (5 CTAs per
@@ -116,18 +159,18 @@ __device__ __forceinline__ void batch_item(const lbm_batch_member_dev* __restric
 #endif
 template <int FRAME, bool FAST>
 __global__ void __maxnreg__(LBM_BATCH_V4_MAXNREG)
-lbm_batch_kernel_v4(const lbm_batch_member_dev* __restrict__ members, const uint2* __restrict__ items,
+lbm_batch_kernel_v4(const lbm_batch_member_dev* __restrict__ members, const BatchItem* __restrict__ items,
                     int nitems, int parity, int pf) {
     batch_item<4, FRAME, FAST>(members, items, nitems, parity, pf);
 }
 template <int FRAME, bool FAST>
 __global__ void __launch_bounds__(256, 4)
-lbm_batch_kernel_v2(const lbm_batch_member_dev* __restrict__ members, const uint2* __restrict__ items,
+lbm_batch_kernel_v2(const lbm_batch_member_dev* __restrict__ members, const BatchItem* __restrict__ items,
                     int nitems, int parity, int pf) {
     batch_item<2, FRAME, FAST>(members, items, nitems, parity, pf);
 }
 
-using BatchKernel = void (*)(const lbm_batch_member_dev*, const uint2*, int, int, int);
+using BatchKernel = void (*)(const lbm_batch_member_dev*, const BatchItem*, int, int, int);
 
 BatchKernel pick_kernel(int V, int frame, int fast) {
     if (V == 2) {
@@ -173,12 +216,17 @@ int ensure_table(lbm_batch* B) {
     }
     if (!changed) return LBM_OK;
     std::vector<lbm_batch_member_dev> host(n);
-    std::vector<uint2> general, rest;
+    std::vector<BatchItem> general, rest;
     std::vector<uint8_t> flags;
     for (int i = 0; i < n; ++i) {
         lbm_lattice* L = B->members[i];
-        host[i].a[0] = lattice_args<float>(L, L->cur, false);
-        host[i].a[1] = lattice_args<float>(L, L->cur ^ 1, false);
+        host[i].a = lattice_args<float>(L, L->cur, false);
+        if (L->pitch % 32 != 0 || L->pitch / 32 >= (1 << 14) || L->w >= (1 << 18) ||
+            L->plane != int64_t(L->pitch) * L->h)
+            return bfail(LBM_ERR_INVALID_ARGUMENT, "batch member row pitch or width out of range");
+        const float* buf0 = static_cast<const float*>(L->buf[L->cur]);
+        const float* buf1 = static_cast<const float*>(L->buf[L->cur ^ 1]);
+        const uint32_t w_pitch = uint32_t(L->w) | (uint32_t(L->pitch / 32) << 18);
         B->built_version[i] = L->version;
         B->built_cur[i] = L->cur;
         flags.resize(size_t(L->h) * L->ntiles);
@@ -193,13 +241,13 @@ int ensure_table(lbm_batch* B) {
                     // interior code with link masks when the member has them
                     const uint32_t kind = fl == 0 ? kInterior : fl == 2 ? kWrap
                                         : (fl == 3 && L->use_links) ? kLinks : kGeneral;
-                    const uint2 item = make_uint2(uint32_t(i) | (kind << 24),
-                                                  (uint32_t(r) << 12) | uint32_t(t));
+                    const BatchItem item{buf0, buf1, uint32_t(i) | (kind << 24),
+                                         (uint32_t(r) << 12) | uint32_t(t), w_pitch, uint32_t(L->h)};
                     (kind == kGeneral ? general : rest).push_back(item);
                 }
     }
     // general items first: their longer latency overlaps the rest
-    std::vector<uint2> tasks(general);
+    std::vector<BatchItem> tasks(general);
     tasks.insert(tasks.end(), rest.begin(), rest.end());
     if (!B->d_members) BATCH_CUDA(cudaMalloc(&B->d_members, sizeof(lbm_batch_member_dev) * n));
     BATCH_CUDA(cudaMemcpyAsync(B->d_members, host.data(), sizeof(lbm_batch_member_dev) * n,
@@ -208,11 +256,11 @@ int ensure_table(lbm_batch* B) {
         if (B->d_tasks) cudaFree(B->d_tasks);
         B->d_tasks = nullptr;
         B->tasks_cap = 0;
-        BATCH_CUDA(cudaMalloc(&B->d_tasks, sizeof(uint2) * tasks.size()));
+        BATCH_CUDA(cudaMalloc(&B->d_tasks, sizeof(BatchItem) * tasks.size()));
         B->tasks_cap = tasks.size();
     }
     if (!tasks.empty())
-        BATCH_CUDA(cudaMemcpyAsync(B->d_tasks, tasks.data(), sizeof(uint2) * tasks.size(),
+        BATCH_CUDA(cudaMemcpyAsync(B->d_tasks, tasks.data(), sizeof(BatchItem) * tasks.size(),
                                    cudaMemcpyHostToDevice, B->stream));
     BATCH_CUDA(cudaStreamSynchronize(B->stream));
     B->ntasks = int(tasks.size());

@@ -430,8 +430,8 @@ __device__ __forceinline__ void collide_cells(const Consts<typename Store<S>::CT
 
 // Writes the V collided cells of a thread and, when requested, their moments
 // (computed from the stored, i.e. encoded, values).
-template <class S, int V, bool FAST>
-__device__ __forceinline__ void store_cells(const StepArgs<typename Store<S>::CT>& a, int y,
+template <class S, int V, bool FAST, class A>
+__device__ __forceinline__ void store_cells(const A& a, int y,
                                             int x0, const S (&enc)[9][V]) {
     using CT = typename Store<S>::CT;
     using ST = Store<S>;
@@ -494,8 +494,8 @@ __device__ __forceinline__ void store_cells(const StepArgs<typename Store<S>::CT
 // L2 now (one bulk prefetch of the warp's 32 V columns per plane, lanes 0-8)
 // and that warp's loads find them there.  Interior tiles only (full tiles, so
 // the range stays inside the row).
-template <class S, int V, int FRAME, class CT>
-__device__ __forceinline__ void prefetch_ahead(const StepArgs<CT>& a, int y, int x0, int lane) {
+template <class S, int V, int FRAME, class A>
+__device__ __forceinline__ void prefetch_ahead(const A& a, int y, int x0, int lane) {
     if (a.pf_rows > 0 && lane < 9) {
         const int ys = y + a.pf_rows - DROW(FRAME, lane);
         if (ys < a.h) {
@@ -527,8 +527,8 @@ __device__ __forceinline__ void zero_past_edge(typename Store<S>::CT (&f)[9][V],
 struct InteriorRows {
     int64_t rm, r0, rp;     // element offsets of rows y - 1, y, y + 1
     int left, right;        // columns x0 - 1 and x0 + V, wrapped
-    template <class CT>
-    __device__ __forceinline__ InteriorRows(const StepArgs<CT>& a, int y, int x0, int V) {
+    template <class A>
+    __device__ __forceinline__ InteriorRows(const A& a, int y, int x0, int V) {
         const int64_t P = a.pitch;
         rm = int64_t(y == 0 ? a.h - 1 : y - 1) * P;
         r0 = int64_t(y) * P;
@@ -547,8 +547,8 @@ struct InteriorRows {
 // same code applies the fixups of step_general from the tile's per-lane link
 // masks: bounce-back links take the cell's own opposite population, solid
 // cells swap (full-way) or keep their populations (half-way).
-template <class S, int V, int FRAME, bool FAST, bool SR = false, bool GEN_CT = false>
-__device__ __forceinline__ void step_interior(const StepArgs<typename Store<S>::CT>& a, int y,
+template <class S, int V, int FRAME, bool FAST, bool SR = false, bool GEN_CT = false, class A>
+__device__ __forceinline__ void step_interior(const A& a, int y,
                                               int x0, int lane, int tile = 0) {
     using CT = typename Store<S>::CT;
     using ST = Store<S>;
@@ -651,8 +651,8 @@ __device__ __forceinline__ void step_interior(const StepArgs<typename Store<S>::
 // collision and 9 vector stores; the edge rows and columns wrap.  Lanes past
 // the edge only feed the shuffles, and the lane holding column w - 1 takes
 // column 0 for the cell whose source lies past the edge.
-template <class S, int V, int FRAME, bool FAST, bool SR = false>
-__device__ __forceinline__ void step_interior_wrap(const StepArgs<typename Store<S>::CT>& a, int y,
+template <class S, int V, int FRAME, bool FAST, bool SR = false, class A>
+__device__ __forceinline__ void step_interior_wrap(const A& a, int y,
                                               int x0, int lane) {
     using CT = typename Store<S>::CT;
     using ST = Store<S>;
@@ -1069,8 +1069,8 @@ __device__ __forceinline__ void step_interior_wrap_packed(const StepArgs<float>&
 // classifies boundary links; phase C fetches the cell's own opposite
 // populations for bounce-back links (only near walls and solids); phase D
 // collides and stores.
-template <class S, int V, int FRAME, bool FAST, bool SR = false, bool EDGE = true>
-__device__ __forceinline__ void step_general(const StepArgs<typename Store<S>::CT>& a, int y,
+template <class S, int V, int FRAME, bool FAST, bool SR = false, bool EDGE = true, class A>
+__device__ __forceinline__ void step_general(const A& a, int y,
                                              int tile, int lane) {
     using CT = typename Store<S>::CT;
     using ST = Store<S>;
