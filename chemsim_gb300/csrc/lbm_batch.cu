@@ -163,8 +163,13 @@ lbm_batch_kernel_v4(const lbm_batch_member_dev* __restrict__ members, const Batc
                     int nitems, int parity, int pf) {
     batch_item<4, FRAME, FAST>(members, items, nitems, parity, pf);
 }
+#ifdef LBM_BATCH_V2_MAXNREG
+template <int FRAME, bool FAST>
+__global__ void __maxnreg__(LBM_BATCH_V2_MAXNREG)
+#else
 template <int FRAME, bool FAST>
 __global__ void __launch_bounds__(256, 4)
+#endif
 lbm_batch_kernel_v2(const lbm_batch_member_dev* __restrict__ members, const BatchItem* __restrict__ items,
                     int nitems, int parity, int pf) {
     batch_item<2, FRAME, FAST>(members, items, nitems, parity, pf);
