@@ -687,8 +687,17 @@ def run_e2e(spec, args, torch, dist, readback="async"):
     lat.set_geometry(spec.solid)
     lat.init_equilibrium(rho, ux, uy)
     lat.step(args.warmup)
-    lat.read_moments_async(*outs[0])          # allocates the staging area outside the timing
-    lat.readback_wait()
+    # untimed: allocate the staging areas and make one transfer into every
+    # host buffer the timed frames use (a buffer's first transfer pays its
+    # host-side mapping setup)
+    for j in range(2):
+        if readback == "mapped":
+            lat.step_moments_to(1, *ptrs[j])
+        elif readback == "frame":
+            lat.render_async(imgs[j], lbm.RENDER_VELOCITY)
+        else:
+            lat.read_moments_async(*outs[j])
+        lat.readback_wait()
     lat.synchronize()
     frames = max(1, args.steps // 2)
     lib = lat._lib
