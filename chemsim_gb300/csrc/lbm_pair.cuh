@@ -79,10 +79,17 @@ __device__ __forceinline__ void collide_fast_x2(const Consts<float>& c, const fl
         const float2 v[5] = {bc2(0.f), ux, uy, d, e};
 #pragma unroll
         for (int i = 1; i < 9; ++i) {
-            // c_i.u of directions 1, 2, 5, 6 is v[1..4]; of their opposites its negation
+            // c_i.u of directions 1, 2, 5, 6 is v[1..4]; of their opposites its
+            // negation.  An opposite's kcF and cF4 are the exact negations of
+            // its partner's (the host computes them from the negated c_i) and
+            // w_i is shared, so four constants of each kind and two gw values
+            // serve all eight directions (fewer registers where the constants
+            // come from memory).
             const int p = (i == 1 || i == 3) ? 1 : (i == 2 || i == 4) ? 2 : (i == 5 || i == 7) ? 3 : 4;
-            const float s = (i == 3 || i == 4 || i == 7 || i == 8) ? -1.f : 1.f;
-            out[i] = fma2(bc2(c.gw[i]), fma2(v[p], bc2(s * c.cF4[i]), sub2(bc2(c.kcF[i]), uF)), out[i]);
+            const int r = p == 1 ? 1 : p == 2 ? 2 : p == 3 ? 5 : 6;
+            const bool opp = i == 3 || i == 4 || i == 7 || i == 8;
+            const float kc = opp ? -c.kcF[r] : c.kcF[r];
+            out[i] = fma2(bc2(c.gw[i < 5 ? 1 : 5]), fma2(v[p], bc2(c.cF4[r]), sub2(bc2(kc), uF)), out[i]);
         }
         out[0] = fma2(bc2(c.gw[0]), sub2(bc2(c.kcF[0]), uF), out[0]);
     }
@@ -141,9 +148,12 @@ __device__ __forceinline__ void collide_dev_x2_general(const Consts<float>& c,
         const float2 v[5] = {bc2(0.f), ux, uy, d, e};
 #pragma unroll
         for (int i = 1; i < 9; ++i) {
+            // the shared constants of collide_fast_x2
             const int p = (i == 1 || i == 3) ? 1 : (i == 2 || i == 4) ? 2 : (i == 5 || i == 7) ? 3 : 4;
-            const float s = (i == 3 || i == 4 || i == 7 || i == 8) ? -1.f : 1.f;
-            out[i] = fma2(bc2(c.sgw[i]), fma2(v[p], bc2(s * c.cF4[i]), sub2(bc2(c.kcF[i]), uF)), out[i]);
+            const int r = p == 1 ? 1 : p == 2 ? 2 : p == 3 ? 5 : 6;
+            const bool opp = i == 3 || i == 4 || i == 7 || i == 8;
+            const float kc = opp ? -c.kcF[r] : c.kcF[r];
+            out[i] = fma2(bc2(c.sgw[i < 5 ? 1 : 5]), fma2(v[p], bc2(c.cF4[r]), sub2(bc2(kc), uF)), out[i]);
         }
         out[0] = fma2(bc2(c.sgw[0]), sub2(bc2(c.kcF[0]), uF), out[0]);
     }
