@@ -19,14 +19,18 @@
 // (the 3 x (32V + 2) neighbourhood is fluid and inside the lattice, or wraps
 // at periodic edges: no boundary logic), 2 = the same for the partial last
 // tile of a periodic row, 1 = the general path with the full boundary
-// treatment (non-periodic edges), 3 = the general path without edge handling
-// (solids nearby, every source cell inside the lattice).  Tiles 1 and 3 are listed
-// and run first.  Interior warps also prefetch into L2 the rows that warps
+// treatment (non-periodic edges), 3 = solids nearby, every source cell inside
+// the lattice.  Tiles 1 are listed and run first (the general path); tiles 3
+// run in place on the interior code with per-lane link masks where the
+// lattice has them (f32, 16-bit at 8 cells per thread), else they are listed
+// too and take the general path without edge handling.  Interior warps also
+// prefetch into L2 the rows that warps
 // further down the row-major wavefront will pull.  The flags and the list
 // are rebuilt whenever the geometry or the tile width changes.
 #pragma once
 
 #include <array>
+#include <type_traits>
 
 #include "lbm_common.cuh"
 #include "lbm_pair.cuh"
